@@ -1,0 +1,382 @@
+"""Benchmark: D3Q19 A-A lid-driven cavity, MLUPS on GB300.
+
+Workload (default): the 384^3 FP32 lid-driven cavity (lid u_x = 0.05,
+Re = 1000, nu = 0.0192, tau = 0.5576), initialised at rest.  One bench
+"step" is one lattice time step over the whole domain (alpha on even
+counters, beta on odd, as src/CController.cpp:1278-1287 alternates them);
+MLUPS counts interior cells x steps (src/CController.cpp:1463-1464).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--storage f32|f64|f16s|bf16s] [--size 384]
+
+Prints ONE JSON line (rank 0).  Keys beyond the base contract:
+  roofline      -- dominant kernel's algorithmic bytes / CUDA-event time vs
+                   the measured HBM copy bandwidth (MEASURED_PEAKS.json)
+  cpu_baseline  -- the CPU oracle (a port of the reference kernels, OpenMP
+                   over all host cores) on a bounded slab of the same domain
+  e2e           -- the same job through the C ABI with pinned host buffers:
+                   upload of the full population state, K steps, download of
+                   density and velocity fields, all inside the timed region
+  clocks        -- SM clocks and throttle reasons sampled during timing
+N > 1 (torchrun): independent replicas, one cavity per GPU ("replicas
+only": the single-domain path has no exchange step), max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_VALUE = {"f64": 8, "f32": 4, "f16s": 2, "bf16s": 2}
+DTYPE_NAME = {"f64": "f64", "f32": "f32", "f16s": "f16 (shifted, fp32 collide)", "bf16s": "bf16 (shifted, fp32 collide)"}
+METRIC = "MLUPS"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--storage", default="f32", choices=list(BYTES_PER_VALUE))
+    ap.add_argument("--size", type=int, default=384)
+    ap.add_argument("--lid", type=float, default=0.05)
+    ap.add_argument("--nu", type=float, default=0.0192)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def config_dict(a, world):
+    return {"workload": f"lid-driven cavity {a.size}^3 {a.storage}, Re={a.size * a.lid / a.nu:.0f}, "
+                        f"u_lid={a.lid}, nu={a.nu}", "domain": [a.size] * 3, "storage": a.storage,
+            "step": "one lattice time step (alpha/beta alternating), whole domain",
+            "l2": f"inputs larger than L2: {19 * (a.size + 2) ** 3 * BYTES_PER_VALUE[a.storage] / 1e9:.2f} GB "
+                  f"population array vs {L2_BYTES / 1e6:.0f} MB L2",
+            "parallelism": f"replicas x{world}" if world > 1 else "single domain, 1 GPU"}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle as the checker/baseline only)
+# ---------------------------------------------------------------------------
+
+def cpu_run(a, seconds_target, steps_max=None, use_reference=True):
+    """Time the reference algorithm on host cores over z-slabs of the domain.
+
+    Uses the reference's own CPU kernels (oracle/_ref) where they were built
+    (only possible where the reference checkout exists), else the C port
+    (oracle/liblbm_oracle.so) with OpenMP over all cores.  Returns
+    (mlups, cores, kind, sample)."""
+    from oracle import oracle as orc
+
+    dtype = np.float64 if a.storage == "f64" else np.float32
+    kind = "port"
+    lib = None
+    if use_reference and os.path.exists(orc.REF_SO):
+        try:
+            lib, kind = orc.Reference(), "reference"
+        except OSError:
+            lib = None
+    if lib is None:
+        orc.build()
+        lib = orc.Oracle()
+    cores = lib.num_threads() if kind == "port" else 1
+    n = a.size
+    _, itau = orc.tau_of(a.nu, dtype)
+    lid = dtype(a.lid)
+    dd, flags = lib.init(n, n, n, dtype)
+    flags[1:-1, n, 1:-1] = orc.VELOCITY_INJECTION
+    # calibrate slab thickness on one alpha/beta pair of 2 planes
+    probe = (1, 1, 1), (n, n, min(2, n))
+    t0 = time.perf_counter()
+    lib.alpha(dd, flags, itau, lid, origin=probe[0], size=probe[1])
+    lib.beta(dd, flags, itau, lid, origin=probe[0], size=probe[1])
+    rate = 2 * n * n * probe[1][2] / max(time.perf_counter() - t0, 1e-6)
+    steps = 10 if steps_max is None else steps_max
+    planes = int(max(1, min(n, seconds_target * rate / (steps * n * n))))
+    o, s = (1, 1, 1), (n, n, planes)
+    t0 = time.perf_counter()
+    for i in range(steps):
+        if i & 1:
+            lib.beta(dd, flags, itau, lid, origin=o, size=s)
+        else:
+            lib.alpha(dd, flags, itau, lid, origin=o, size=s)
+    dt = time.perf_counter() - t0
+    mlups = n * n * planes * steps / dt / 1e6
+    sample = (f"{steps} steps over a {n}x{n}x{planes} interior slab of the {n}^3 domain "
+              f"({n * n * planes * steps / 1e6:.1f} M lattice updates, {dt:.1f} s)")
+    return mlups, cores, kind, sample
+
+
+def reference_arm(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+
+    dtype = np.float64 if a.storage == "f64" else np.float32
+    use_ref = os.path.exists(orc.REF_SO)
+    lib = orc.Reference() if use_ref else None
+    if lib is None:
+        orc.build()
+        lib = orc.Oracle()
+    kind = "reference" if use_ref else "port"
+    cores = 1 if use_ref else lib.num_threads()
+    n = a.size
+    _, itau = orc.tau_of(a.nu, dtype)
+    lid = dtype(a.lid)
+    dd, flags = lib.init(n, n, n, dtype)
+    flags[1:-1, n, 1:-1] = orc.VELOCITY_INJECTION
+    # per-step sample: a z-slab sized so K+W steps take about two minutes
+    probe = (1, 1, 1), (n, n, min(2, n))
+    t0 = time.perf_counter()
+    lib.alpha(dd, flags, itau, lid, origin=probe[0], size=probe[1])
+    lib.beta(dd, flags, itau, lid, origin=probe[0], size=probe[1])
+    rate = 2 * n * n * probe[1][2] / max(time.perf_counter() - t0, 1e-6)
+    budget = 120.0 / max(1, a.steps + a.warmup)
+    planes = int(max(1, min(n, budget * rate / (n * n))))
+    o, s = (1, 1, 1), (n, n, planes)
+    for i in range(a.warmup):
+        (lib.beta if i & 1 else lib.alpha)(dd, flags, itau, lid, origin=o, size=s)
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        j = a.warmup + i
+        (lib.beta if j & 1 else lib.alpha)(dd, flags, itau, lid, origin=o, size=s)
+    dt = time.perf_counter() - t0
+    value = n * n * planes * a.steps / dt / 1e6
+    sample = f"each step: one lattice update of a {n}x{n}x{planes} slab of the {n}^3 domain"
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": round(dt / a.steps * 1e3, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_NAME[a.storage], "data": "synthetic",
+            "config": config_dict(a, world), "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id: str):
+        self.device_id = device_id
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.device_id, f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(a, kernel):
+    """dram bytes per launch from a committed ncu summary, if one matches."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    key = f"{kernel}:{a.storage}"
+    if key not in d:
+        return None
+    e = d[key]
+    # scaled from the captured case to this domain by interior cells
+    return e["dram_bytes_per_launch"] * (a.size ** 3) / float(e["cells"])
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+        return
+    run_gpu(a)
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_gpu(a):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cavityflow_cuda_gb300 import CLbmSolverGB300, derive_lattice, kernel_launches
+
+    n = a.size
+    lat = derive_lattice(velocity=(a.lid, 0, 0), viscosity=a.nu, domain_size=(n, n, n), timestep=1.0,
+                         storage=a.storage)
+    bpv = BYTES_PER_VALUE[a.storage]
+    bytes_per_lup = 2 * 19 * bpv
+    stream = torch.cuda.Stream()
+    props = torch.cuda.get_device_properties(local)
+    dev_id = str(getattr(props, "uuid", "")) or str(local)
+    if dev_id and not dev_id.startswith("GPU-") and len(dev_id) == 36:
+        dev_id = "GPU-" + dev_id
+
+    with CLbmSolverGB300((n, n, n), lat["inv_tau"], lat["velocity"][0], storage=a.storage, device=local) as s:
+        assert s.info()["fast_path"] == 1
+        # warm-up (also captures the run graph)
+        s.run(max(a.warmup, 3), stream=stream)
+        stream.synchronize()
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = kernel_launches()
+        with ClockSampler(dev_id) as clocks:
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            s.run(a.steps, stream=stream)
+            ev1.record(stream)
+            ev1.synchronize()
+        launches = kernel_launches() - l0
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        barrier(world)
+        total_lups = float(n) ** 3 * a.steps * world
+        value = total_lups / (ms / 1e3) / 1e6
+
+        # per-kernel durations (CUDA events on the launching stream)
+        per = {"alpha": [], "beta": []}
+        for i in range(20):
+            kind = "beta" if s.info()["last_step_was_alpha"] else "alpha"
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            (s.simulationStepBeta if kind == "beta" else s.simulationStepAlpha)(stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            per[kind].append(e0.elapsed_time(e1))
+        avg = {k: statistics.mean(v) for k, v in per.items() if v}
+        dom = max(avg, key=avg.get)
+        peak, peak_kind = measured_peaks()
+        algo = bytes_per_lup * float(n) ** 3
+        achieved = algo / (avg[dom] / 1e3) / 1e9
+        traffic = profile_traffic(a, f"{dom}_fast")
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"{dom}_fast<{a.storage}>",
+                "algorithmic_bytes_per_launch": algo, "peak_source": f"{peak_kind} hbm_gbs (copy)",
+                "per_kernel_ms": {k: round(v, 4) for k, v in avg.items()},
+                "per_kernel_frac": {k: round(algo / (v / 1e3) / 1e9 / peak, 4) for k, v in avg.items()}}
+
+        # end to end through the C ABI with pinned host buffers
+        e2e = None
+        if not a.no_e2e:
+            state = torch.empty((19, n + 2, n + 2, n + 2), dtype=torch.float64 if a.storage == "f64" else torch.float32,
+                                pin_memory=True)
+            s.getDensityDistributions((0, 0, 0), (n + 2, n + 2, n + 2), out=state.numpy())
+            macro = torch.empty((4, n, n, n), dtype=state.dtype, pin_memory=True)
+            mnp = macro.numpy()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            s.setDensityDistributions(state.numpy(), (0, 0, 0), (n + 2, n + 2, n + 2), stream=stream)
+            s.run(a.steps, stream=stream)
+            stream.synchronize()
+            s.getDensities(out=mnp[0])
+            s.getVelocities(out=mnp[1:])
+            t_e2e = time.perf_counter() - t0
+            e2e = {"value": round(float(n) ** 3 * a.steps / t_e2e / 1e6 * world, 1), "unit": "MLUPS",
+                   "h2d_bytes_per_step": int(state.numel() * state.element_size() / a.steps),
+                   "d2h_bytes_per_step": int(macro.numel() * macro.element_size() / a.steps),
+                   "how": "pinned host -> setDensityDistributions (full state), run(K), getDensities + "
+                          "getVelocities -> pinned host; host wall clock"}
+
+    cpu = None
+    if rank == 0 and not a.no_cpu:
+        mlups, cores, kind, sample = cpu_run(a, a.cpu_seconds, use_reference=False)
+        cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 5), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_NAME[a.storage], "data": "synthetic",
+                "config": config_dict(a, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "clocks": clocks.summary(), "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

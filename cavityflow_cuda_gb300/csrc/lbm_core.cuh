@@ -1,0 +1,251 @@
+// lbm_core.cuh -- lattice, storage layout and collision arithmetic shared by
+// every kernel of the GB300 D3Q19 A-A solver.
+//
+// The translation units that include this header are compiled with
+// -fmad=false: the FP64 and FP32 collisions below then execute exactly the
+// IEEE operations, in the same order, as the reference kernels built for
+// x86-64 (src/gpukernels/lbm_alpha.cu:86-331, src/gpukernels/lbm_beta.cu:98-636,
+// src/common.h:132-160), which gives bit-identical populations.
+#pragma once
+
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+namespace lbm {
+
+constexpr int Q = 19;
+
+// Flag values of src/common.h:54-61 (stored as one byte per cell here).
+enum : uint8_t { kObstacle = 1, kFluid = 2, kInjection = 4, kGhost = 8 };
+
+// D3Q19 ordering of src/common.h:29-47: 0 +x, 1 -x, 2 +y, 3 -y, 4 (+x+y),
+// 5 (-x-y), 6 (+x-y), 7 (-x+y), 8 (+x+z), 9 (-x-z), 10 (+x-z), 11 (-x+z),
+// 12 (+y+z), 13 (-y-z), 14 (+y-z), 15 (-y+z), 16 +z, 17 -z, 18 rest.
+// Opposite directions pair as (2k, 2k+1).
+__host__ __device__ constexpr int dir_x(int k)
+{
+    return k == 0 ? 1 : k == 1 ? -1 : k == 4 ? 1 : k == 5 ? -1 : k == 6 ? 1 : k == 7 ? -1
+         : k == 8 ? 1 : k == 9 ? -1 : k == 10 ? 1 : k == 11 ? -1 : 0;
+}
+__host__ __device__ constexpr int dir_y(int k)
+{
+    return k == 2 ? 1 : k == 3 ? -1 : k == 4 ? 1 : k == 5 ? -1 : k == 6 ? -1 : k == 7 ? 1
+         : k == 12 ? 1 : k == 13 ? -1 : k == 14 ? 1 : k == 15 ? -1 : 0;
+}
+__host__ __device__ constexpr int dir_z(int k)
+{
+    return k == 8 ? 1 : k == 9 ? -1 : k == 10 ? -1 : k == 11 ? 1 : k == 12 ? 1 : k == 13 ? -1
+         : k == 14 ? -1 : k == 15 ? 1 : k == 16 ? 1 : k == 17 ? -1 : 0;
+}
+__host__ __device__ constexpr int opp(int k) { return k == 18 ? 18 : (k ^ 1); }
+
+// Lattice weight of direction k in precision T, folded as the reference
+// writes them: (T)1/(T)18, (T)1/(T)36, (T)1/(T)3.
+template <typename T>
+__host__ __device__ constexpr T weight(int k)
+{
+    return k == 18 ? T(1) / T(3) : (k < 4 || k >= 16) ? T(1) / T(18) : T(1) / T(36);
+}
+
+// ---------------------------------------------------------------------------
+// Device layout of the population array.
+//
+// 19 slots; slot k is a padded 3-D array of (nz+2) planes x (ny+2) rows x P
+// columns.  Cell x of a row (halo coordinates, 0..nx+1) sits at column
+// x + xoff.  xoff = (32 bytes / element) - 1 puts interior cell x = 1 on a
+// 32-byte sector boundary, so each 16-byte vector group of the fast kernels
+// (cells 1+gV .. V+gV, V = 16 bytes / element) is aligned, and each warp's
+// 32 consecutive groups start on a sector.  P leaves room for one scalar
+// access right of the last group and is a multiple of 32 bytes, and every
+// slot starts on a 256-byte boundary.
+// ---------------------------------------------------------------------------
+struct Grid {
+    int nx, ny, nz;      // interior cells
+    int V;               // cells per 16-byte vector
+    int xoff;            // column of halo cell x = 0
+    int G;               // vector groups per row, ceil(nx / V)
+    long long P;         // row pitch (elements)
+    long long PY;        // plane pitch (elements) = P * (ny + 2)
+    long long S;         // slot stride (elements)
+
+    __host__ __device__ long long idx(int x, int y, int z) const
+    {
+        return (long long)z * PY + (long long)y * P + x + xoff;
+    }
+    // Index of a cell in the compact, unpadded reference layout
+    // ((nz+2) x (ny+2) x (nx+2), x fastest) used by flags and macro arrays.
+    __host__ __device__ long long ref(int x, int y, int z) const
+    {
+        return ((long long)z * (ny + 2) + y) * (nx + 2) + x;
+    }
+    __host__ __device__ long long cells() const { return (long long)(nx + 2) * (ny + 2) * (nz + 2); }
+};
+
+inline Grid make_grid(int nx, int ny, int nz, int elem_bytes)
+{
+    Grid g;
+    g.nx = nx; g.ny = ny; g.nz = nz;
+    g.V = 16 / elem_bytes;
+    const int sector = 32 / elem_bytes;
+    g.xoff = sector - 1;
+    g.G = (nx + g.V - 1) / g.V;
+    const long long need = (long long)g.xoff + (long long)g.G * g.V + 2;  // last scalar column + 1
+    g.P = (need + sector - 1) / sector * sector;
+    g.PY = g.P * (ny + 2);
+    const long long slot_align = 256 / elem_bytes;
+    g.S = (g.PY * (nz + 2) + slot_align - 1) / slot_align * slot_align;
+    return g;
+}
+
+// ---------------------------------------------------------------------------
+// Storage types.  F64/F32 hold f_i; F16S/BF16S hold the deviation f_i - w_i
+// as raw 16-bit patterns.  `T` is the arithmetic type of the collision.
+// ---------------------------------------------------------------------------
+struct F64 {
+    using bits = double;
+    using T = double;
+    static constexpr bool shifted = false;
+    __device__ static T load(bits b) { return b; }
+    __device__ static bits store(T v) { return v; }
+};
+struct F32 {
+    using bits = float;
+    using T = float;
+    static constexpr bool shifted = false;
+    __device__ static T load(bits b) { return b; }
+    __device__ static bits store(T v) { return v; }
+};
+struct F16S {
+    using bits = unsigned short;
+    using T = float;
+    static constexpr bool shifted = true;
+    __device__ static T load(bits b) { return __half2float(__ushort_as_half(b)); }
+    __device__ static bits store(T v) { return __half_as_ushort(__float2half_rn(v)); }
+};
+struct BF16S {
+    using bits = unsigned short;
+    using T = float;
+    static constexpr bool shifted = true;
+    __device__ static T load(bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+    __device__ static bits store(T v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
+};
+
+// Scalar lattice parameters of one domain.
+struct Params {
+    double inv_tau;
+    double lid_u;
+    double gx, gy, gz;
+};
+
+// ---------------------------------------------------------------------------
+// Collision arithmetic (operation order of the reference, see file header).
+// ---------------------------------------------------------------------------
+
+// Density and momentum, each accumulator in the order of
+// src/gpukernels/lbm_alpha.cu:86-186.
+template <typename T>
+__device__ __forceinline__ void moments(const T* f, T& rho, T& vx, T& vy, T& vz)
+{
+    T r = f[0], x = f[0], y, z;
+    r += f[1];  x -= f[1];
+    r += f[2];  y = f[2];
+    r += f[3];  y -= f[3];
+    r += f[4];  x += f[4];  y += f[4];
+    r += f[5];  x -= f[5];  y -= f[5];
+    r += f[6];  x += f[6];  y -= f[6];
+    r += f[7];  x -= f[7];  y += f[7];
+    r += f[8];  x += f[8];  z = f[8];
+    r += f[9];  x -= f[9];  z -= f[9];
+    r += f[10]; x += f[10]; z -= f[10];
+    r += f[11]; x -= f[11]; z += f[11];
+    r += f[12]; y += f[12]; z += f[12];
+    r += f[13]; y -= f[13]; z -= f[13];
+    r += f[14]; y += f[14]; z -= f[14];
+    r += f[15]; y -= f[15]; z += f[15];
+    r += f[16]; z += f[16];
+    r += f[17]; z -= f[17];
+    r += f[18];
+    rho = r; vx = x; vy = y; vz = z;
+}
+
+// Incompressible equilibrium, src/common.h:132-160.
+template <typename T>
+__device__ __forceinline__ void pair_eq(T w, T P, T s, T& plus, T& minus)
+{
+    const T s2 = s * s;
+    plus = w * (P + T(3) * s + (T(9) / T(2)) * s2);
+    minus = w * (P + T(-3) * s + (T(9) / T(2)) * s2);
+}
+
+template <typename T>
+__device__ __forceinline__ void equilibrium(T rho, T vx, T vy, T vz, T* e)
+{
+    const T vel2 = vx * vx + vy * vy + vz * vz;
+    const T P = rho - (T(3) / T(2)) * vel2;
+    const T wa = T(1) / T(18), wd = T(1) / T(36);
+    pair_eq(wa, P, vx, e[0], e[1]);
+    pair_eq(wa, P, vy, e[2], e[3]);
+    pair_eq(wd, P, vx + vy, e[4], e[5]);
+    pair_eq(wd, P, vx - vy, e[6], e[7]);
+    pair_eq(wd, P, vx + vz, e[8], e[9]);
+    pair_eq(wd, P, vx - vz, e[10], e[11]);
+    pair_eq(wd, P, vy + vz, e[12], e[13]);
+    pair_eq(wd, P, vy - vz, e[14], e[15]);
+    pair_eq(wa, P, vz, e[16], e[17]);
+    e[18] = (T(1) / T(3)) * P;
+}
+
+// Alpha-step gravity (src/gpukernels/lbm_alpha.cu:213-326).  In the reference
+// each term is stored in `tmp`, a #define for `rho` (lbm_alpha.cu:203), so each
+// term after the first scales the previous term; reproduced as written.
+template <typename T>
+__device__ __forceinline__ void alpha_gravity(T* f, T rho, T gx, T gy, T gz)
+{
+    const T wa = T(1) / T(18), wd = T(1) / T(36);
+    T t = gx * wa * rho;                    f[1] -= t;  f[0] += t;
+    t = gy * (T(-1) / T(18)) * t;           f[3] -= t;  f[2] += t;
+    t = (gx - gy) * wd * t;                 f[5] -= t;  f[4] += t;
+    t = (gx + gy) * wd * t;                 f[7] -= t;  f[6] += t;
+    t = (gx + gz) * wd * t;                 f[9] -= t;  f[8] += t;
+    t = (gx - gz) * wd * t;                 f[11] -= t; f[10] += t;
+    t = (gz - gy) * wd * t;                 f[13] -= t; f[12] += t;
+    t = (gz + gy) * (T(-1) / T(36)) * t;    f[15] -= t; f[14] += t;
+    t = gz * wa * t;                        f[17] -= t; f[16] += t;
+}
+
+// BGK collision of a FLUID cell in place (lbm_alpha.cu:209-331,
+// lbm_beta.cu:574-636).  For shifted storage f holds f - w and the same
+// arithmetic yields the post-collision deviation: with rho the density
+// deviation, feq(rho) - w is exactly the reference formula.
+template <typename T>
+__device__ __forceinline__ void collide_fluid(T* f, T inv_tau)
+{
+    T rho, vx, vy, vz, e[Q];
+    moments(f, rho, vx, vy, vz);
+    equilibrium(rho, vx, vy, vz, e);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] += inv_tau * (e[k] - f[k]);
+}
+
+template <typename T>
+__device__ __forceinline__ void collide_fluid_gravity(T* f, T inv_tau, T gx, T gy, T gz)
+{
+    T rho, vx, vy, vz, e[Q];
+    moments(f, rho, vx, vy, vz);
+    equilibrium(rho, vx, vy, vz, e);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[k] += inv_tau * (e[k] - f[k]);
+    alpha_gravity(f, rho, gx, gy, gz);
+}
+
+// VELOCITY_INJECTION: feq(rho = 1, j = (U, 0, 0)) (lbm_alpha.cu:376-511,
+// lbm_beta.cu:661-732); rho0 = 0 gives the deviation form for shifted storage.
+template <typename T>
+__device__ __forceinline__ void inject(T* f, T rho0, T lid_u)
+{
+    equilibrium(rho0, lid_u, T(0), T(0), f);
+}
+
+}  // namespace lbm

@@ -1,0 +1,671 @@
+// lbm_kernels.cu -- sm_103a kernels of the D3Q19 A-A lid-driven cavity.
+//
+// Hot path (box cavity, flags implied by coordinates):
+//   alpha_fast  -- src/gpukernels/lbm_alpha.cu:22-532 restated: each thread
+//                  owns one 16-byte group of V consecutive cells of an x row,
+//                  reads their 19 slots with 128-bit loads, collides and
+//                  writes every population to its opposite slot.
+//   beta_fast   -- src/gpukernels/lbm_beta.cu:32-915 restated: the same
+//                  thread pulls the 19 incoming populations from the
+//                  neighbours' slots, collides and pushes the results back to
+//                  the same addresses.  Rows shifted by +-1 in x are
+//                  realigned with warp shuffles; the lanes at a warp or row
+//                  edge use scalar accesses for the one element that leaves
+//                  the warp.
+// General path (any flags, cuboid sub-steps, gravity): one cell per thread,
+// reads the per-cell flag (alpha_general / beta_general).
+#include <cstdint>
+#include <type_traits>
+#include <utility>
+
+#include "lbm_core.cuh"
+#include "lbm_kernels.h"
+
+namespace lbm {
+
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f)
+{
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+// 16-byte vector access in storage type St, converted to the arithmetic type.
+template <class St>
+struct Vio {
+    using bits = typename St::bits;
+    using T = typename St::T;
+    static constexpr int V = 16 / sizeof(bits);
+    union Pack {
+        uint4 u;
+        bits b[V];
+    };
+    __device__ static void load(const bits* p, T (&a)[V])
+    {
+        Pack x;
+        x.u = *reinterpret_cast<const uint4*>(p);
+#pragma unroll
+        for (int v = 0; v < V; ++v) a[v] = St::load(x.b[v]);
+    }
+    __device__ static void store(bits* p, const T (&a)[V])
+    {
+        Pack x;
+#pragma unroll
+        for (int v = 0; v < V; ++v) x.b[v] = St::store(a[v]);
+        *reinterpret_cast<uint4*>(p) = x.u;
+    }
+};
+
+// ===========================================================================
+// Fast path
+// ===========================================================================
+
+template <class St>
+__global__ void __launch_bounds__(kFastBlock) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                         const typename St::T inv_tau,
+                                                         const typename St::T lid_u, const int lid_y)
+{
+    using T = typename St::T;
+    using IO = Vio<St>;
+    constexpr int V = IO::V;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)g.G * g.ny * g.nz;
+    if (t >= total) return;
+    const int gi = (int)(t % g.G);
+    const long long row = t / g.G;
+    const int y = 1 + (int)(row % g.ny);
+    const int z = 1 + (int)(row / g.ny);
+    const int x0 = 1 + gi * V;
+    const long long base = g.idx(x0, y, z);
+
+    T f[Q][V];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) IO::load(dd + k * g.S + base, f[k]);
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
+        T c[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) c[k] = f[k][v];
+        if (lid) inject(c, rho0, lid_u);
+        else collide_fluid(c, inv_tau);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[opp(k)][v] = c[k];  // population k -> slot opp(k)
+    }
+#pragma unroll
+    for (int k = 0; k < Q; ++k) IO::store(dd + k * g.S + base, f[k]);
+}
+
+template <class St>
+__global__ void __launch_bounds__(kFastBlock) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                        const typename St::T inv_tau,
+                                                        const typename St::T lid_u, const int lid_y)
+{
+    using T = typename St::T;
+    using IO = Vio<St>;
+    constexpr int V = IO::V;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long total = (long long)g.G * g.ny * g.nz;
+    const bool active = t < total;
+    const int lane = threadIdx.x & 31;
+    const long long tt = active ? t : 0;
+    const int gi = (int)(tt % g.G);
+    const long long row = tt / g.G;
+    const int y = 1 + (int)(row % g.ny);
+    const int z = 1 + (int)(row / g.ny);
+    const int x0 = 1 + gi * V;
+    // The neighbouring group of the same row is held by the adjacent lane.
+    const bool left_in = gi > 0 && lane > 0;
+    const bool right_in = gi < g.G - 1 && lane < 31;
+    const unsigned full = 0xffffffffu;
+
+    // p[k][v]: value of slot k at (cell x0+v) + c_k, i.e. population opp(k)
+    // arriving at cell x0+v.  edge[k]: the aligned element of slot k that lies
+    // outside this thread's shifted window (kept to rewrite it unchanged).
+    T p[Q][V];
+    T edge[Q];
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        T a[V];
+        if (active) IO::load(dd + rb, a);
+        else {
+#pragma unroll
+            for (int v = 0; v < V; ++v) a[v] = T(0);
+        }
+        if constexpr (cx == 0) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) p[k][v] = a[v];
+            edge[k] = T(0);
+        } else if constexpr (cx == 1) {
+            T nb = __shfl_down_sync(full, a[0], 1);
+            if (active && !right_in) nb = St::load(dd[rb + V]);
+#pragma unroll
+            for (int v = 0; v < V - 1; ++v) p[k][v] = a[v + 1];
+            p[k][V - 1] = nb;
+            edge[k] = a[0];
+        } else {
+            T pb = __shfl_up_sync(full, a[V - 1], 1);
+            if (active && !left_in) pb = St::load(dd[rb - 1]);
+            p[k][0] = pb;
+#pragma unroll
+            for (int v = 1; v < V; ++v) p[k][v] = a[v - 1];
+            edge[k] = a[V - 1];
+        }
+    });
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+#pragma unroll
+    for (int v = 0; v < V; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
+        T c[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) c[opp(k)] = p[k][v];
+        if (lid) inject(c, rho0, lid_u);
+        else collide_fluid(c, inv_tau);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) p[k][v] = c[k];  // population k -> slot k at x + c_k
+    }
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        if constexpr (cx == 0) {
+            if (active) IO::store(dd + rb, p[k]);
+        } else if constexpr (cx == 1) {
+            // aligned element 0 belongs to cell x0-1 (left lane's last cell)
+            const T from_left = __shfl_up_sync(full, p[k][V - 1], 1);
+            if (active) {
+                T o[V];
+#pragma unroll
+                for (int v = 1; v < V; ++v) o[v] = p[k][v - 1];
+                if (left_in || gi == 0) {
+                    o[0] = left_in ? from_left : edge[k];
+                    IO::store(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 1; v < V; ++v) dd[rb + v] = St::store(o[v]);
+                }
+                if (!right_in && x0 + V - 1 <= g.nx) dd[rb + V] = St::store(p[k][V - 1]);
+            }
+        } else {
+            // aligned element V-1 belongs to cell x0+V (right lane's first cell)
+            const T from_right = __shfl_down_sync(full, p[k][0], 1);
+            if (active) {
+                T o[V];
+#pragma unroll
+                for (int v = 0; v < V - 1; ++v) o[v] = p[k][v + 1];
+                if (right_in || gi == g.G - 1) {
+                    o[V - 1] = right_in ? from_right : edge[k];
+                    IO::store(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < V - 1; ++v) dd[rb + v] = St::store(o[v]);
+                }
+                if (!left_in) dd[rb - 1] = St::store(p[k][0]);
+            }
+        }
+    });
+}
+
+// ===========================================================================
+// General path: flag array, cuboid, gravity, halo cells with any flag
+// ===========================================================================
+
+// Position of slot k touched by halo cell (x, y, z) in the beta step: the
+// reference wraps the linear index modulo the cell count (DOMAIN_WRAP,
+// src/gpukernels/lbm_beta.cu:22-25, :59-64).
+__device__ __forceinline__ long long wrapped_position(const Grid& g, int x, int y, int z, int k)
+{
+    const long long X = g.nx + 2, XY = X * (g.ny + 2), C = XY * (g.nz + 2);
+    const int cx = dir_x(k), cy = dir_y(k), cz = dir_z(k);
+    long long d = (cx > 0 ? 1 : cx < 0 ? C - 1 : 0) + (cy > 0 ? X : cy < 0 ? C - X : 0) +
+                  (cz > 0 ? XY : cz < 0 ? C - XY : 0);
+    const long long lin = (g.ref(x, y, z) + d) % C;
+    const int zn = (int)(lin / XY);
+    const int yn = (int)((lin / X) % (g.ny + 2));
+    const int xn = (int)(lin % X);
+    return g.idx(xn, yn, zn);
+}
+
+template <class St, bool kGravity>
+__global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t* __restrict__ flags,
+                              const Grid g, const Params prm, const int3 o, const int3 s)
+{
+    using T = typename St::T;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)s.x * s.y * s.z;
+    if (t >= n) return;
+    const int x = o.x + (int)(t % s.x);
+    const int y = o.y + (int)((t / s.x) % s.y);
+    const int z = o.z + (int)(t / ((long long)s.x * s.y));
+    const uint8_t fl = flags[g.ref(x, y, z)];
+    if (fl != kFluid && fl != kInjection) return;  // OBSTACLE, GHOST: untouched
+    const long long c0 = g.idx(x, y, z);
+    const T inv_tau = T(prm.inv_tau);
+    T f[Q];
+    if (fl == kFluid) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[k] = St::load(dd[k * g.S + c0]);
+        if (kGravity) collide_fluid_gravity(f, inv_tau, T(prm.gx), T(prm.gy), T(prm.gz));
+        else collide_fluid(f, inv_tau);
+    } else {
+        inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
+        if (kGravity) alpha_gravity(f, T(1), T(prm.gx), T(prm.gy), T(prm.gz));
+    }
+#pragma unroll
+    for (int k = 0; k < Q; ++k) dd[opp(k) * g.S + c0] = St::store(f[k]);
+}
+
+template <class St>
+__global__ void beta_general(typename St::bits* __restrict__ dd, const uint8_t* __restrict__ flags,
+                             const Grid g, const Params prm, const int3 o, const int3 s)
+{
+    using T = typename St::T;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long n = (long long)s.x * s.y * s.z;
+    if (t >= n) return;
+    const int x = o.x + (int)(t % s.x);
+    const int y = o.y + (int)((t / s.x) % s.y);
+    const int z = o.z + (int)(t / ((long long)s.x * s.y));
+    const uint8_t fl = flags[g.ref(x, y, z)];
+    if (fl == kObstacle) return;  // swaps then writes back what it read: a no-op
+    const bool interior = x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz;
+    long long pos[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k)
+        pos[k] = k * g.S + (interior ? g.idx(x + dir_x(k), y + dir_y(k), z + dir_z(k))
+                                     : wrapped_position(g, x, y, z, k));
+    T f[Q];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) f[opp(k)] = St::load(dd[pos[k]]);
+    if (fl == kFluid) collide_fluid(f, T(prm.inv_tau));
+    else if (fl == kInjection) inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
+    // GHOST_LAYER (and any other value): streamed through unchanged
+#pragma unroll
+    for (int k = 0; k < Q; ++k) dd[pos[k]] = St::store(f[k]);
+}
+
+// ===========================================================================
+// Initialisation, flags, macroscopic fields, reductions, packing
+// ===========================================================================
+
+template <class St>
+__global__ void init_populations(typename St::bits* __restrict__ dd, const Grid g)
+{
+    using T = typename St::T;
+    const long long n = (long long)Q * g.S;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(i / g.S);
+        // feq(rho = 1, u = 0) evaluated as src/gpukernels/lbm_init.cu:97-193 does
+        T e[Q];
+        equilibrium(T(1), T(0), T(0), T(0), e);
+        T v = T(0);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (q == k) v = e[q];
+        dd[i] = St::store(St::shifted ? T(0) : v);
+    }
+}
+
+__global__ void init_flags(uint8_t* __restrict__ flags, const Grid g, const Bc bc)
+{
+    const long long n = g.cells();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int X = g.nx + 2, Y = g.ny + 2, Z = g.nz + 2;
+        const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((long long)X * Y));
+        // src/gpukernels/lbm_init.cu:73-93: an OBSTACLE face wins over later faces
+        int fl = kFluid;
+        if (x == 0) fl = bc.f[0];
+        if (x == X - 1 && fl != kObstacle) fl = bc.f[1];
+        if (y == 0 && fl != kObstacle) fl = bc.f[2];
+        if (y == Y - 1 && fl != kObstacle) fl = bc.f[3];
+        if (z == 0 && fl != kObstacle) fl = bc.f[4];
+        if (z == Z - 1 && fl != kObstacle) fl = bc.f[5];
+        flags[i] = (uint8_t)fl;
+    }
+}
+
+// Counts cells that differ from the box cavity with all-obstacle halo:
+// counts[0] against "lid plane y = ny", counts[1] against "no lid".
+__global__ void check_cavity_flags(const uint8_t* __restrict__ flags, const Grid g,
+                                   unsigned long long* __restrict__ counts)
+{
+    unsigned long long bad_lid = 0, bad_nolid = 0;
+    const long long n = g.cells();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int X = g.nx + 2, Y = g.ny + 2;
+        const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((long long)X * Y));
+        const bool halo = x == 0 || x > g.nx || y == 0 || y > g.ny || z == 0 || z > g.nz;
+        const uint8_t fl = flags[i];
+        const uint8_t want_nolid = halo ? kObstacle : kFluid;
+        const uint8_t want_lid = halo ? kObstacle : (y == g.ny ? kInjection : kFluid);
+        bad_lid += fl != want_lid;
+        bad_nolid += fl != want_nolid;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        bad_lid += __shfl_down_sync(0xffffffffu, bad_lid, off);
+        bad_nolid += __shfl_down_sync(0xffffffffu, bad_nolid, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (bad_lid) atomicAdd(&counts[0], bad_lid);
+        if (bad_nolid) atomicAdd(&counts[1], bad_nolid);
+    }
+}
+
+// Post-collision populations of interior cell (x,y,z) after the last step:
+// after alpha they sit swapped in the cell's own slots, after beta in slot k
+// of the neighbour x + c_k.  Returned in arithmetic type (deviation form for
+// shifted storage).
+template <class St>
+__device__ __forceinline__ void post_populations(const typename St::bits* dd, const Grid& g, int x, int y,
+                                                 int z, bool last_alpha, typename St::T* f)
+{
+    const long long c0 = g.idx(x, y, z);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const long long p = last_alpha ? opp(k) * g.S + c0
+                                       : k * g.S + g.idx(x + dir_x(k), y + dir_y(k), z + dir_z(k));
+        f[k] = St::load(dd[p]);
+    }
+}
+
+// Density and velocity (u = j) of the time level collided last, on the full
+// grid in the compact reference layout: out[0] rho, out[1..3] j.
+template <class St>
+__global__ void compute_macros(const typename St::bits* __restrict__ dd, const uint8_t* __restrict__ flags,
+                               const Grid g, const bool last_alpha, const typename St::T lid_u,
+                               typename St::T* __restrict__ out)
+{
+    using T = typename St::T;
+    const long long n = g.cells();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int X = g.nx + 2, Y = g.ny + 2;
+        const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((long long)X * Y));
+        const bool interior = x >= 1 && x <= g.nx && y >= 1 && y <= g.ny && z >= 1 && z <= g.nz;
+        const uint8_t fl = flags[i];
+        T r = T(0), vx = T(0), vy = T(0), vz = T(0);
+        if (interior && fl == kFluid) {
+            T f[Q];
+            post_populations<St>(dd, g, x, y, z, last_alpha, f);
+            moments(f, r, vx, vy, vz);
+            if (St::shifted) r = r + T(1);
+        } else if (interior && fl == kInjection) {
+            r = T(1);
+            vx = lid_u;
+        }
+        out[i] = r;
+        out[n + i] = vx;
+        out[2 * n + i] = vy;
+        out[3 * n + i] = vz;
+    }
+}
+
+// FP64 mass and momentum, pass 1: one partial sum per block (warp shuffles,
+// then a fixed-order combine of the warps), so the result is deterministic.
+// Mass counts every live slot: the 19 own slots of each active (FLUID or
+// lid) interior cell, plus the slots of inactive neighbours (walls) that its
+// pushes land in, where a population waits one step before it returns; the
+// steps conserve that sum exactly.  Momentum is that of the cells'
+// post-collision populations.
+template <class St>
+__global__ void __launch_bounds__(kReduceBlock) reduce_partials(const typename St::bits* __restrict__ dd,
+                                                                const uint8_t* __restrict__ flags,
+                                                                const Grid g, const bool last_alpha,
+                                                                double* __restrict__ partials)
+{
+    using T = typename St::T;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(i % g.nx);
+        const int y = 1 + (int)((i / g.nx) % g.ny);
+        const int z = 1 + (int)(i / ((long long)g.nx * g.ny));
+        const uint8_t fl = flags[g.ref(x, y, z)];
+        if (fl != kFluid && fl != kInjection) continue;
+        const long long c0 = g.idx(x, y, z);
+        double m = 0.0;
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const double w = St::shifted ? (double)weight<float>(k) : 0.0;
+            m += (double)St::load(dd[k * g.S + c0]) + w;
+            const int xn = x + dir_x(k), yn = y + dir_y(k), zn = z + dir_z(k);
+            const uint8_t fn = flags[g.ref(xn, yn, zn)];
+            if (fn != kFluid && fn != kInjection) m += (double)St::load(dd[k * g.S + g.idx(xn, yn, zn)]) + w;
+        }
+        T f[Q];
+        post_populations<St>(dd, g, x, y, z, last_alpha, f);
+        double px = 0.0, py = 0.0, pz = 0.0;
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const double v = (double)f[k];
+            px += dir_x(k) * v;
+            py += dir_y(k) * v;
+            pz += dir_z(k) * v;
+        }
+        acc[0] += m; acc[1] += px; acc[2] += py; acc[3] += pz;
+    }
+    __shared__ double warp_sums[kReduceBlock / 32][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        for (int off = 16; off > 0; off >>= 1) acc[q] += __shfl_down_sync(0xffffffffu, acc[q], off);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int q = 0; q < 4; ++q) warp_sums[w][q] = acc[q];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double s = 0.0;
+        for (int i = 0; i < kReduceBlock / 32; ++i) s += warp_sums[i][threadIdx.x];
+        partials[blockIdx.x * 4 + threadIdx.x] = s;
+    }
+}
+
+// Pass 2: thread q sums column q of the partials in block order.
+__global__ void reduce_final(const double* __restrict__ partials, int nblocks, double* __restrict__ out)
+{
+    if (threadIdx.x < 4) {
+        double s = 0.0;
+        for (int b = 0; b < nblocks; ++b) s += partials[b * 4 + threadIdx.x];
+        out[threadIdx.x] = s;
+    }
+}
+
+// Cuboid of one slot <-> packed host-type buffer, unshifting (f = s + w) on
+// the way out and shifting on the way in for 16-bit storage.
+template <class St>
+__global__ void pack_slot(const typename St::bits* __restrict__ dd, const Grid g, int k, const int3 o,
+                          const int3 s, float* __restrict__ out)
+{
+    const long long n = (long long)s.x * s.y * s.z;
+    const float w = weight<float>(k);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int x = o.x + (int)(t % s.x), y = o.y + (int)((t / s.x) % s.y);
+        const int z = o.z + (int)(t / ((long long)s.x * s.y));
+        const float v = St::load(dd[k * g.S + g.idx(x, y, z)]);
+        out[t] = St::shifted ? v + w : v;
+    }
+}
+
+template <class St>
+__global__ void unpack_slot(typename St::bits* __restrict__ dd, const Grid g, int k, const int3 o,
+                            const int3 s, const float* __restrict__ in)
+{
+    const long long n = (long long)s.x * s.y * s.z;
+    const float w = weight<float>(k);
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int x = o.x + (int)(t % s.x), y = o.y + (int)((t / s.x) % s.y);
+        const int z = o.z + (int)(t / ((long long)s.x * s.y));
+        const float v = in[t];
+        dd[k * g.S + g.idx(x, y, z)] = St::store(St::shifted ? v - w : v);
+    }
+}
+
+// ===========================================================================
+// Host-side launchers
+// ===========================================================================
+
+namespace {
+
+long long g_launches = 0;
+
+int grid_for(long long n, int block, int cap = 1 << 30)
+{
+    long long b = (n + block - 1) / block;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+template <class F>
+cudaError_t with_storage(int storage, F&& f)
+{
+    switch (storage) {
+    case 0: return f(F64{});
+    case 1: return f(F32{});
+    case 2: return f(F16S{});
+    case 3: return f(BF16S{});
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+long long kernel_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAXED); }
+
+void add_launches(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
+
+static void count_launch(int n = 1) { add_launches(n); }
+
+cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st)
+{
+    cudaError_t e = with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        init_populations<St><<<grid_for((long long)Q * g.S, 256, 4096), 256, 0, st>>>(
+            static_cast<typename St::bits*>(dd), g);
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    init_flags<<<grid_for(g.cells(), 256, 4096), 256, 0, st>>>(flags, g, bc);
+    count_launch(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts,
+                                cudaStream_t st)
+{
+    check_cavity_flags<<<grid_for(g.cells(), 256, 4096), 256, 0, st>>>(flags, g, counts);
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fast_step(int storage, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                             cudaStream_t st)
+{
+    const long long threads = (long long)g.G * g.ny * g.nz;
+    const int blocks = grid_for(threads, kFastBlock);
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        using T = typename St::T;
+        auto* d = static_cast<typename St::bits*>(dd);
+        if (alpha) alpha_fast<St><<<blocks, kFastBlock, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+        else beta_fast<St><<<blocks, kFastBlock, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,
+                                const Params& p, int3 o, int3 s, cudaStream_t st)
+{
+    const long long n = (long long)s.x * s.y * s.z;
+    const int blocks = grid_for(n, 128);
+    const bool gravity = p.gx != 0.0 || p.gy != 0.0 || p.gz != 0.0;
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        auto* d = static_cast<typename St::bits*>(dd);
+        if (alpha && gravity) alpha_general<St, true><<<blocks, 128, 0, st>>>(d, flags, g, p, o, s);
+        else if (alpha) alpha_general<St, false><<<blocks, 128, 0, st>>>(d, flags, g, p, o, s);
+        else beta_general<St><<<blocks, 128, 0, st>>>(d, flags, g, p, o, s);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
+                          double lid_u, void* out, cudaStream_t st)
+{
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        using T = typename St::T;
+        compute_macros<St><<<grid_for(g.cells(), 256, 8192), 256, 0, st>>>(
+            static_cast<const typename St::bits*>(dd), flags, g, last_alpha, T(lid_u), static_cast<T*>(out));
+        return cudaGetLastError();
+    });
+}
+
+int reduce_blocks(const Grid& g)
+{
+    return grid_for((long long)g.nx * g.ny * g.nz, kReduceBlock, kReduceMaxBlocks);
+}
+
+cudaError_t launch_reduce(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
+                          double* partials, double* out, cudaStream_t st)
+{
+    const int blocks = reduce_blocks(g);
+    cudaError_t e = with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        reduce_partials<St><<<blocks, kReduceBlock, 0, st>>>(static_cast<const typename St::bits*>(dd), flags,
+                                                              g, last_alpha, partials);
+        return cudaGetLastError();
+    });
+    if (e != cudaSuccess) return e;
+    reduce_final<<<1, 32, 0, st>>>(partials, blocks, out);
+    count_launch(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_slot(int storage, const void* dd, const Grid& g, int k, int3 o, int3 s, float* out,
+                             cudaStream_t st)
+{
+    const long long n = (long long)s.x * s.y * s.z;
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        pack_slot<St><<<grid_for(n, 256, 8192), 256, 0, st>>>(static_cast<const typename St::bits*>(dd), g, k,
+                                                               o, s, out);
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_unpack_slot(int storage, void* dd, const Grid& g, int k, int3 o, int3 s, const float* in,
+                               cudaStream_t st)
+{
+    const long long n = (long long)s.x * s.y * s.z;
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        unpack_slot<St><<<grid_for(n, 256, 8192), 256, 0, st>>>(static_cast<typename St::bits*>(dd), g, k, o, s,
+                                                                 in);
+        return cudaGetLastError();
+    });
+}
+
+}  // namespace lbm

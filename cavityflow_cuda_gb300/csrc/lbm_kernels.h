@@ -1,0 +1,41 @@
+// lbm_kernels.h -- host-side launch interface of the solver's kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lbm_core.cuh"
+
+namespace lbm {
+
+constexpr int kFastBlock = 256;       // threads per block, vectorised step kernels
+constexpr int kReduceBlock = 256;     // threads per block, FP64 reduction
+constexpr int kReduceMaxBlocks = 1024;
+
+// Face flags of the six halo faces: -x, +x, -y, +y, -z, +z.
+struct Bc {
+    int f[6];
+};
+
+// Kernel launches queued by this library since load, and a correction for
+// launches that were captured into a graph rather than run.
+long long kernel_launches();
+void add_launches(long long n);
+
+cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
+cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
+cudaError_t launch_fast_step(int storage, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                             cudaStream_t st);
+cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,
+                                const Params& p, int3 origin, int3 size, cudaStream_t st);
+cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
+                          double lid_u, void* out, cudaStream_t st);
+int reduce_blocks(const Grid& g);
+cudaError_t launch_reduce(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
+                          double* partials, double* out, cudaStream_t st);
+cudaError_t launch_pack_slot(int storage, const void* dd, const Grid& g, int k, int3 origin, int3 size,
+                             float* out, cudaStream_t st);
+cudaError_t launch_unpack_slot(int storage, void* dd, const Grid& g, int k, int3 origin, int3 size,
+                               const float* in, cudaStream_t st);
+
+}  // namespace lbm

@@ -1,0 +1,304 @@
+"""Python binding of the solver's C ABI (include/lbm_gb300.h) via ctypes.
+
+``CLbmSolverGB300`` mirrors the method names and argument meaning of the
+reference's ``CLbmSolverGPU<T>`` (src/CLbmSolverGPU.cuh:25-95): alpha/beta
+steps over the whole domain or a cuboid, and get/set of populations, flags,
+velocities and densities over cuboids in halo coordinates.  Where the
+reference asserts or exits, these methods raise ``LbmError``.
+
+The library is the in-tree ``liblbm_gb300.so``; importing this module does
+not load it, constructing a solver does, and fails loudly if it is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+from typing import Optional, Sequence
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "liblbm_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "lbm_gb300.h")
+
+OBSTACLE, FLUID, VELOCITY_INJECTION, GHOST_LAYER = 1, 2, 4, 8
+DIRECTION_ALL, LEFT, RIGHT, BOTTOM, TOP, BACK, FRONT = -1, 0, 1, 2, 3, 4, 5
+STORAGE = {"f64": 0, "f32": 1, "f16s": 2, "bf16s": 3}
+
+_lib: Optional[C.CDLL] = None
+
+
+class LbmError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+
+
+class _Physical(C.Structure):
+    _fields_ = [("velocity", C.c_double * 3), ("acceleration", C.c_double * 3), ("viscosity", C.c_double),
+                ("max_velocity", C.c_double), ("max_acceleration", C.c_double), ("domain_size", C.c_int32 * 3),
+                ("domain_length", C.c_double * 3), ("timestep", C.c_double)]
+
+
+class _Lattice(C.Structure):
+    _fields_ = [("timestep", C.c_double), ("tau", C.c_double), ("inv_tau", C.c_double),
+                ("velocity", C.c_double * 3), ("acceleration", C.c_double * 3), ("viscosity", C.c_double)]
+
+
+class _Params(C.Structure):
+    _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("boundary", C.c_int32 * 6),
+                ("inv_tau", C.c_double), ("lid_velocity", C.c_double), ("gravity", C.c_double * 3),
+                ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class _Info(C.Structure):
+    _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("value_size", C.c_int32),
+                ("vector_cells", C.c_int32), ("step_counter", C.c_int64), ("last_step_was_alpha", C.c_int32),
+                ("fast_path", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
+                ("device_bytes", C.c_int64)]
+
+
+def declared_functions() -> list[str]:
+    """Names of the functions include/lbm_gb300.h declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lbm_[a-z0-9_]+)\s*\(", text)))
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load liblbm_gb300.so; raise if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m cavityflow_cuda_gb300.build`")
+    lib = C.CDLL(path)
+    P, I, I64, V = C.c_void_p, C.c_int, C.c_int64, C.c_void_p
+    sig = {
+        "lbm_derive_lattice": ([P, C.c_int32, P], I),
+        "lbm_create": ([P, P], I),
+        "lbm_destroy": ([V], I),
+        "lbm_get_info": ([V, P], I),
+        "lbm_get_domain": ([V, P], I),
+        "lbm_value_size": ([V], I),
+        "lbm_set_driven_cavity": ([V], I),
+        "lbm_step_alpha": ([V, P], I),
+        "lbm_step_alpha_cuboid": ([V, P, P, P], I),
+        "lbm_step_beta": ([V, P], I),
+        "lbm_step_beta_cuboid": ([V, P, P, P], I),
+        "lbm_run": ([V, I64, P], I),
+        "lbm_synchronize": ([V], I),
+        "lbm_get_density_distributions": ([V, P, P, P, P], I),
+        "lbm_set_density_distributions": ([V, P, P, C.c_int32, P, P], I),
+        "lbm_get_flags": ([V, P, P, P], I),
+        "lbm_set_flags": ([V, P, P, P], I),
+        "lbm_get_velocities": ([V, P, P, P], I),
+        "lbm_set_velocities": ([V, P, P, P], I),
+        "lbm_get_densities": ([V, P, P, P], I),
+        "lbm_set_densities": ([V, P, P, P], I),
+        "lbm_reduce": ([V, P, P], I),
+        "lbm_status_string": ([I], C.c_char_p),
+        "lbm_last_error": ([], C.c_char_p),
+        "lbm_kernel_launches": ([], I64),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        lib = load_library()
+        raise LbmError(status, f"{lib.lbm_status_string(status).decode()}: {lib.lbm_last_error().decode()}")
+
+
+def _stream_ptr(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream or None
+    return int(getattr(stream, "cuda_stream"))
+
+
+def _i3(v: Optional[Sequence[int]]):
+    return None if v is None else (C.c_int32 * 3)(*[int(t) for t in v])
+
+
+def kernel_launches() -> int:
+    return int(load_library().lbm_kernel_launches())
+
+
+def derive_lattice(velocity=(0.05, 0.0, 0.0), acceleration=(0.0, 0.0, 0.0), viscosity=0.032, max_velocity=0.1,
+                   max_acceleration=0.1, domain_size=(64, 64, 64), domain_length=None, timestep=1.0,
+                   storage: str = "f32") -> dict:
+    """Lattice parameters from physical ones, as src/CLbmSolver.cpp:28-327 derives them."""
+    lib = load_library()
+    ph = _Physical()
+    ph.velocity[:] = list(velocity)
+    ph.acceleration[:] = list(acceleration)
+    ph.viscosity = viscosity
+    ph.max_velocity = max_velocity
+    ph.max_acceleration = max_acceleration
+    ph.domain_size[:] = list(domain_size)
+    ph.domain_length[:] = list(domain_length if domain_length is not None else domain_size)
+    ph.timestep = timestep
+    out = _Lattice()
+    _check(lib.lbm_derive_lattice(C.byref(ph), STORAGE[storage], C.byref(out)))
+    return dict(timestep=out.timestep, tau=out.tau, inv_tau=out.inv_tau, velocity=tuple(out.velocity),
+                acceleration=tuple(out.acceleration), viscosity=out.viscosity)
+
+
+class CLbmSolverGB300:
+    """One D3Q19 domain on one GPU, driven through the C ABI."""
+
+    def __init__(self, size: Sequence[int], inv_tau: float, lid_velocity: float, storage: str = "f32",
+                 boundary: Sequence[int] = (OBSTACLE,) * 6, gravity: Sequence[float] = (0.0, 0.0, 0.0),
+                 device: int = 0, driven_cavity: bool = True):
+        self._lib = load_library()
+        p = _Params()
+        p.size[:] = [int(s) for s in size]
+        p.storage = STORAGE[storage]
+        p.boundary[:] = [int(b) for b in boundary]
+        p.inv_tau = float(inv_tau)
+        p.lid_velocity = float(lid_velocity)
+        p.gravity[:] = [float(g) for g in gravity]
+        p.device = int(device)
+        h = C.c_void_p()
+        _check(self._lib.lbm_create(C.byref(p), C.byref(h)))
+        self._h = h
+        self.storage = storage
+        self.size = tuple(int(s) for s in size)
+        self.dtype = np.float64 if storage == "f64" else np.float32
+        if driven_cavity:
+            self.setDrivenCavity()
+
+    # -- lifecycle --------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def info(self) -> dict:
+        i = _Info()
+        _check(self._lib.lbm_get_info(self._h, C.byref(i)))
+        return {f: (tuple(getattr(i, f)) if f == "size" else getattr(i, f)) for f, _ in _Info._fields_}
+
+    def getDomain(self) -> tuple:
+        return self.size
+
+    def setDrivenCavity(self) -> None:
+        _check(self._lib.lbm_set_driven_cavity(self._h))
+
+    # -- steps ------------------------------------------------------------
+    def simulationStepAlpha(self, origin=None, size=None, stream=None) -> None:
+        if origin is None and size is None:
+            _check(self._lib.lbm_step_alpha(self._h, _stream_ptr(stream)))
+        else:
+            _check(self._lib.lbm_step_alpha_cuboid(self._h, _i3(origin), _i3(size), _stream_ptr(stream)))
+
+    def simulationStepBeta(self, origin=None, size=None, stream=None) -> None:
+        if origin is None and size is None:
+            _check(self._lib.lbm_step_beta(self._h, _stream_ptr(stream)))
+        else:
+            _check(self._lib.lbm_step_beta_cuboid(self._h, _i3(origin), _i3(size), _stream_ptr(stream)))
+
+    def run(self, steps: int, stream=None) -> None:
+        _check(self._lib.lbm_run(self._h, int(steps), _stream_ptr(stream)))
+
+    def synchronize(self) -> None:
+        _check(self._lib.lbm_synchronize(self._h))
+
+    # -- data -------------------------------------------------------------
+    def _shape(self, size, comps):
+        if size is None:
+            size = self.size
+        return (comps, size[2], size[1], size[0]) if comps > 1 else (size[2], size[1], size[0])
+
+    def getDensityDistributions(self, origin=None, size=None, out: Optional[np.ndarray] = None, stream=None,
+                                sync: bool = True) -> np.ndarray:
+        if out is None:
+            out = np.empty(self._shape(size, 19), dtype=self.dtype)
+        assert out.flags.c_contiguous and out.dtype == self.dtype and out.size == int(np.prod(self._shape(size, 19)))
+        _check(self._lib.lbm_get_density_distributions(self._h, _i3(origin), _i3(size), out.ctypes.data,
+                                                       _stream_ptr(stream)))
+        if sync:
+            self.synchronize()
+        return out
+
+    def setDensityDistributions(self, src: np.ndarray, origin=None, size=None, direction: int = DIRECTION_ALL,
+                                stream=None, sync: bool = True) -> None:
+        src = np.ascontiguousarray(src, dtype=self.dtype)
+        _check(self._lib.lbm_set_density_distributions(self._h, _i3(origin), _i3(size), int(direction),
+                                                       src.ctypes.data, _stream_ptr(stream)))
+        if sync:
+            self.synchronize()
+
+    def getFlags(self, origin=None, size=None) -> np.ndarray:
+        out = np.empty(self._shape(size, 1), dtype=np.int32)
+        _check(self._lib.lbm_get_flags(self._h, _i3(origin), _i3(size), out.ctypes.data))
+        return out
+
+    def setFlags(self, src: np.ndarray, origin=None, size=None) -> None:
+        src = np.ascontiguousarray(src, dtype=np.int32)
+        _check(self._lib.lbm_set_flags(self._h, _i3(origin), _i3(size), src.ctypes.data))
+
+    def getVelocities(self, origin=None, size=None, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self._shape(size, 3), dtype=self.dtype)
+        assert out.flags.c_contiguous and out.dtype == self.dtype and out.size == int(np.prod(self._shape(size, 3)))
+        _check(self._lib.lbm_get_velocities(self._h, _i3(origin), _i3(size), out.ctypes.data))
+        return out
+
+    def setVelocities(self, src: np.ndarray, origin=None, size=None) -> None:
+        src = np.ascontiguousarray(src, dtype=self.dtype)
+        _check(self._lib.lbm_set_velocities(self._h, _i3(origin), _i3(size), src.ctypes.data))
+
+    def getDensities(self, origin=None, size=None, out: Optional[np.ndarray] = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self._shape(size, 1), dtype=self.dtype)
+        assert out.flags.c_contiguous and out.dtype == self.dtype and out.size == int(np.prod(self._shape(size, 1)))
+        _check(self._lib.lbm_get_densities(self._h, _i3(origin), _i3(size), out.ctypes.data))
+        return out
+
+    def setDensities(self, src: np.ndarray, origin=None, size=None) -> None:
+        src = np.ascontiguousarray(src, dtype=self.dtype)
+        _check(self._lib.lbm_set_densities(self._h, _i3(origin), _i3(size), src.ctypes.data))
+
+    def reduce(self, stream=None) -> np.ndarray:
+        """FP64 (mass, momentum x, y, z) of the last collided time level."""
+        out = np.zeros(4, dtype=np.float64)
+        _check(self._lib.lbm_reduce(self._h, out.ctypes.data, _stream_ptr(stream)))
+        return out
+
+    # -- whole-array helpers in the reference layout (halo included) -------
+    def get_all(self) -> np.ndarray:
+        n = self.size
+        return self.getDensityDistributions((0, 0, 0), (n[0] + 2, n[1] + 2, n[2] + 2))
+
+    def set_all(self, dd: np.ndarray) -> None:
+        n = self.size
+        self.setDensityDistributions(dd, (0, 0, 0), (n[0] + 2, n[1] + 2, n[2] + 2))
+
+    def flags_all(self) -> np.ndarray:
+        n = self.size
+        return self.getFlags((0, 0, 0), (n[0] + 2, n[1] + 2, n[2] + 2))

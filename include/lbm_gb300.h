@@ -1,0 +1,247 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300-native D3Q19 A-A lattice-Boltzmann
+ * lid-driven-cavity solver (drop-in for the solver of
+ * saleemayman/cavityflow_cuda).
+ *
+ * Every entry point is plain C: opaque handles, integer status codes, plain
+ * pointers and sizes.  Nothing here exits the process; where the reference
+ * asserts or calls exit() the call returns a status instead (see
+ * lbm_status_string and lbm_last_error).
+ *
+ * Conventions shared with the reference solver interface
+ * (src/CLbmSolver.hpp:30-89, src/CLbmSolverGPU.cuh:25-95):
+ *   - A domain of nx*ny*nz interior cells carries a one-cell halo, so
+ *     "halo coordinates" run 0..n+1 on each axis.  Cuboid arguments
+ *     (origin, size) are in halo coordinates; passing NULL for both selects
+ *     the interior, origin (1,1,1) and size (nx,ny,nz)
+ *     (src/CLbmSolverGPU.cu:597-604).
+ *   - Host buffers are packed [component][z][y][x], x fastest, with
+ *     size[0]*size[1]*size[2] elements per component: 19 components for
+ *     populations, 3 for velocities, 1 for densities and flags.
+ *   - Host values have the solver's value type: double for LBM_STORAGE_F64,
+ *     float for every other storage (lbm_value_size()).
+ *   - Population slots are returned raw, as the reference does: after an
+ *     alpha step they are in the swapped (opposite-slot) convention.
+ *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy default
+ *     stream, as a NULL cudaStream_t* is in the reference.
+ *
+ * Lattice directions, flag values and directions of the direction-filtered
+ * copy are the reference's (src/common.h:29-71).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_GB300_ABI_VERSION 1
+
+/* ---- status codes -------------------------------------------------------- */
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_ERR_INVALID_ARGUMENT = 1, /* bad pointer, size, enum or flag value        */
+    LBM_ERR_OUT_OF_BOUNDS = 2,    /* cuboid outside the domain (reference: assert) */
+    LBM_ERR_CUDA = 3,             /* a CUDA runtime call or launch failed          */
+    LBM_ERR_OUT_OF_MEMORY = 4,    /* device or pinned-host allocation failed       */
+    LBM_ERR_UNSUPPORTED = 5,      /* valid request this build does not provide     */
+    LBM_ERR_CONFIG = 6,           /* no stable time step (reference: exit())       */
+    LBM_ERR_IO = 7,               /* file could not be read or written             */
+    LBM_ERR_BUDGET = 8,           /* request does not fit the memory budget        */
+    LBM_ERR_NOT_READY = 9,        /* result requested before it exists             */
+    LBM_ERR_NO_DEVICE = 10        /* no CUDA device visible                        */
+} lbm_status;
+
+/* Flag values, src/common.h:54-61. */
+enum { LBM_OBSTACLE = 1, LBM_FLUID = 2, LBM_VELOCITY_INJECTION = 4, LBM_GHOST_LAYER = 8 };
+
+/* Faces of the direction-filtered population copy, src/common.h:63-71.
+ * LBM_DIRECTION_ALL selects the unfiltered copy. */
+enum { LBM_DIRECTION_ALL = -1, LBM_LEFT = 0, LBM_RIGHT = 1, LBM_BOTTOM = 2, LBM_TOP = 3,
+       LBM_BACK = 4, LBM_FRONT = 5 };
+
+/* Storage precision of the population array.  F64 and F32 reproduce the
+ * reference kernels' arithmetic exactly.  F16S and BF16S store the
+ * deviation f_i - w_i in 16 bits and collide in FP32 registers. */
+typedef enum lbm_storage {
+    LBM_STORAGE_F64 = 0,
+    LBM_STORAGE_F32 = 1,
+    LBM_STORAGE_F16S = 2,
+    LBM_STORAGE_BF16S = 3
+} lbm_storage;
+
+/* ---- parameters ----------------------------------------------------------- */
+
+/* Physical description, the fields of the reference's XML configuration
+ * that its solver base class reads (src/CConfiguration.hpp:57-104). */
+typedef struct lbm_physical {
+    double velocity[3];         /* lid velocity (m/s); only x drives the lid  */
+    double acceleration[3];     /* external acceleration (m/s^2)              */
+    double viscosity;           /* m^2/s; <= 0 selects the Re=1000 default    */
+    double max_velocity;        /* max dimensionless velocity                 */
+    double max_acceleration;    /* max dimensionless acceleration             */
+    int32_t domain_size[3];     /* cells                                      */
+    double domain_length[3];    /* m                                          */
+    double timestep;            /* s                                          */
+} lbm_physical;
+
+/* Lattice-unit parameters the solver runs on. */
+typedef struct lbm_lattice {
+    double timestep;            /* possibly rescaled time step (s)            */
+    double tau;                 /* BGK relaxation time                        */
+    double inv_tau;             /* 1/tau as the kernels use it                */
+    double velocity[3];         /* dimensionless velocity; [0] drives the lid */
+    double acceleration[3];     /* dimensionless gravity of the alpha step    */
+    double viscosity;           /* dimensionless viscosity                    */
+} lbm_lattice;
+
+/* Derives lattice parameters from physical ones exactly as
+ * CLbmSolver<T>::CLbmSolver does (src/CLbmSolver.cpp:28-327), in the
+ * precision of `storage` (double for F64, float otherwise): default viscosity
+ * from Re = 1000, time-step rescaling for velocity, acceleration and tau
+ * limits [0.51, 1.9] (src/constants.h:26-30).  Where the reference exit()s
+ * (no stable time step) this returns LBM_ERR_CONFIG.  Replaces the
+ * constructor body of src/CLbmSolver.cpp:28-327. */
+int lbm_derive_lattice(const lbm_physical* phys, int32_t storage, lbm_lattice* out);
+
+/* Creation parameters of one solver. */
+typedef struct lbm_params {
+    int32_t size[3];            /* interior cells nx, ny, nz (domain-size)     */
+    int32_t storage;            /* lbm_storage                                 */
+    int32_t boundary[6];        /* face flags: -x, +x, -y, +y, -z, +z
+                                   (src/CLbmSolver.hpp:36-45)                  */
+    double inv_tau;             /* 1/tau                                       */
+    double lid_velocity;        /* x velocity imposed on injection cells       */
+    double gravity[3];          /* dimensionless acceleration (alpha step)     */
+    int32_t device;             /* CUDA device ordinal; the reference picks
+                                   id % nGPUs (src/CLbmSolverGPU.cu:42-45)     */
+    int32_t reserved[3];        /* zero                                        */
+} lbm_params;
+
+typedef struct lbm_solver lbm_solver;   /* opaque */
+
+/* Information about a live solver. */
+typedef struct lbm_info {
+    int32_t size[3];            /* interior cells                              */
+    int32_t storage;
+    int32_t value_size;         /* bytes per host value (4 or 8)               */
+    int32_t vector_cells;       /* cells per 16-byte vector of the fast path   */
+    int64_t step_counter;       /* steps taken (alpha on even, beta on odd)    */
+    int32_t last_step_was_alpha;
+    int32_t fast_path;          /* 1: flags match the box cavity, so the
+                                   vectorised kernels run; 0: flag-array path  */
+    int64_t row_pitch;          /* elements per padded x row on the device     */
+    int64_t slot_stride;        /* elements per population slot                */
+    int64_t device_bytes;       /* bytes of device memory the solver holds     */
+} lbm_info;
+
+/* ---- lifecycle ------------------------------------------------------------ */
+
+/* Allocates the population and flag arrays on `params->device` and
+ * initialises them: flags from the six face conditions, populations at rest
+ * (rho = 1, u = 0).  Replaces CLbmSolverGPU<T>::CLbmSolverGPU
+ * (src/CLbmSolverGPU.cu:30-160) and the lbm_init kernel
+ * (src/gpukernels/lbm_init.cu:41-208). */
+int lbm_create(const lbm_params* params, lbm_solver** out);
+
+/* Frees everything the solver holds.  Replaces
+ * CLbmSolverGPU<T>::~CLbmSolverGPU (src/CLbmSolverGPU.cu:162-171). */
+int lbm_destroy(lbm_solver* solver);
+
+int lbm_get_info(const lbm_solver* solver, lbm_info* info);
+
+/* Interior size, replacing CLbmSolver<T>::getDomain()->getSize()
+ * (src/CLbmSolver.cpp:329-333). */
+int lbm_get_domain(const lbm_solver* solver, int32_t size[3]);
+
+/* Bytes per host value: 8 for F64 storage, 4 otherwise. */
+int lbm_value_size(const lbm_solver* solver);
+
+/* Marks the lid plane y = ny (x in [1,nx], z in [1,nz]) as
+ * VELOCITY_INJECTION.  Replaces CController<T>::setDrivenCavitySzenario
+ * (src/CController.cpp:1289-1348). */
+int lbm_set_driven_cavity(lbm_solver* solver);
+
+/* ---- time steps -------------------------------------------------------------
+ * Kernels are queued on `stream` and the call returns without waiting, as in
+ * the reference. */
+
+/* Whole domain.  Replaces CLbmSolverGPU<T>::simulationStepAlpha(stream)
+ * (src/CLbmSolverGPU.cu:173-248). */
+int lbm_step_alpha(lbm_solver* solver, void* stream);
+/* Cuboid in halo coordinates.  Replaces simulationStepAlpha(origin, size,
+ * stream) (src/CLbmSolverGPU.cu:250-337). */
+int lbm_step_alpha_cuboid(lbm_solver* solver, const int32_t origin[3], const int32_t size[3],
+                          void* stream);
+/* Replaces simulationStepBeta(stream) (src/CLbmSolverGPU.cu:339-419). */
+int lbm_step_beta(lbm_solver* solver, void* stream);
+/* Replaces simulationStepBeta(origin, size, stream)
+ * (src/CLbmSolverGPU.cu:421-513). */
+int lbm_step_beta_cuboid(lbm_solver* solver, const int32_t origin[3], const int32_t size[3],
+                         void* stream);
+
+/* `steps` time steps, alpha on an even counter and beta on an odd one,
+ * replacing the loop of CController<T>::run / computeNextStep
+ * (src/CController.cpp:1278-1287, :1407-1412).  Long runs replay a CUDA
+ * graph of captured alpha/beta pairs. */
+int lbm_run(lbm_solver* solver, int64_t steps, void* stream);
+
+/* Waits for all work queued by the solver. */
+int lbm_synchronize(lbm_solver* solver);
+
+/* ---- data access ------------------------------------------------------------ */
+
+/* Raw population slots of a cuboid to host, asynchronous on `stream` like
+ * the reference's cudaMemcpy3DAsync.  Replaces getDensityDistributions
+ * (src/CLbmSolverGPU.cu:515-611). */
+int lbm_get_density_distributions(lbm_solver* solver, const int32_t origin[3], const int32_t size[3],
+                                  void* host, void* stream);
+/* Host to raw population slots of a cuboid.  `direction` LBM_DIRECTION_ALL
+ * copies all 19 slots (src/CLbmSolverGPU.cu:745-819); a face value copies
+ * only the slots whose lattice vector points into the domain from that face
+ * (src/CLbmSolverGPU.cu:613-714).  Host layout is 19 packed components
+ * either way. */
+int lbm_set_density_distributions(lbm_solver* solver, const int32_t origin[3], const int32_t size[3],
+                                  int32_t direction, const void* host, void* stream);
+
+/* Flags of a cuboid (int32 per cell, the Flag enum).  Synchronous, as the
+ * reference's cudaMemcpy3D.  Replaces getFlags/setFlags
+ * (src/CLbmSolverGPU.cu:821-985).  setFlags accepts only the four Flag
+ * values and switches the solver between the vectorised and the
+ * flag-array kernels as needed. */
+int lbm_get_flags(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], int32_t* host);
+int lbm_set_flags(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], const int32_t* host);
+
+/* Velocity (3 components, the incompressible form u = j) and density of a
+ * cuboid, synchronous.  The values are those of the time level collided
+ * last, computed on demand from the populations; lid cells report
+ * (1, U, 0, 0) and obstacle and halo cells zero.  Values written by the
+ * setters are returned by the getters until the next time step, which
+ * recomputes them, as the reference's stored arrays behave.  Replace
+ * get/setVelocities and get/setDensities (src/CLbmSolverGPU.cu:987-1327). */
+int lbm_get_velocities(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], void* host);
+int lbm_set_velocities(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], const void* host);
+int lbm_get_densities(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], void* host);
+int lbm_set_densities(lbm_solver* solver, const int32_t origin[3], const int32_t size[3], const void* host);
+
+/* FP64 totals over interior FLUID and lid cells of the post-collision
+ * populations of the last step: out = {mass, momentum x, y, z}.  A
+ * deterministic two-pass reduction; synchronous.  No counterpart in the
+ * reference (it has no reduction); it carries the mass-conservation check. */
+int lbm_reduce(lbm_solver* solver, double out[4], void* stream);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+const char* lbm_status_string(int status);
+/* Detail message of the last failing call on this thread ("" if none). */
+const char* lbm_last_error(void);
+/* Number of kernel launches this library has queued since load (all
+ * solvers); the benchmark reports it as its launch count. */
+int64_t lbm_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

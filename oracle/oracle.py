@@ -1,0 +1,204 @@
+"""ctypes access to the CPU oracles.  TEST INFRASTRUCTURE ONLY.
+
+Two libraries, both driven through the same small interface:
+
+* ``liblbm_oracle.so`` -- this repository's C restatement of the reference's
+  A-A kernels (oracle/lbm_oracle.c).  Builds on any host.
+* ``_ref/libref_cavity.so`` -- the reference's own CPU kernels
+  (src/cpukernels/CLbm{Init,Alpha,Beta}CPU.cpp) compiled from the reference
+  checkout by ``make -C oracle ref``.  Exists only where that checkout exists.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline legs may
+import this module, and only as the checker.
+
+Arrays use the reference layout: populations ``(19, nz+2, ny+2, nx+2)``,
+flags ``(nz+2, ny+2, nx+2)`` int32, x fastest.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liblbm_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_cavity.so")
+
+OBSTACLE, FLUID, VELOCITY_INJECTION, GHOST_LAYER = 1, 2, 4, 8
+
+_P = C.c_void_p
+_I = C.c_int
+
+
+def build(ref_src: str | None = None) -> None:
+    """Build liblbm_oracle.so (always) and the reference harness when ``ref_src`` exists."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref_src and os.path.isdir(ref_src):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+def _i3(v):
+    return (C.c_int32 * 3)(*[int(t) for t in v])
+
+
+class _Lib:
+    """Shared calling code for both libraries (same argument conventions)."""
+
+    prefix = ""
+
+    def __init__(self, path: str):
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        self.lib = C.CDLL(path)
+        self.path = path
+
+    def _fn(self, name: str, dtype):
+        sfx = "d" if np.dtype(dtype) == np.float64 else "f"
+        return getattr(self.lib, f"{self.prefix}_{name}_{sfx}")
+
+    @staticmethod
+    def _real(dtype):
+        return C.c_double if np.dtype(dtype) == np.float64 else C.c_float
+
+    def init(self, nx, ny, nz, dtype, bc=(OBSTACLE,) * 6):
+        dd = np.zeros((19, nz + 2, ny + 2, nx + 2), dtype=dtype)
+        flags = np.zeros((nz + 2, ny + 2, nx + 2), dtype=np.int32)
+        fn = self._fn("init", dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, (C.c_int32 * 6)(*bc))
+        return dd, flags
+
+
+class Oracle(_Lib):
+    """The C restatement (oracle/lbm_oracle.c)."""
+
+    prefix = "orc"
+
+    def __init__(self, path: str = ORACLE_SO):
+        super().__init__(path)
+
+    def num_threads(self) -> int:
+        return int(self.lib.orc_num_threads())
+
+    def set_num_threads(self, n: int) -> None:
+        self.lib.orc_set_num_threads(int(n))
+
+    def set_lid(self, flags: np.ndarray) -> None:
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        self.lib.orc_set_lid.argtypes = [_P, _I, _I, _I]
+        self.lib.orc_set_lid(_ptr(flags), nx, ny, nz)
+
+    def alpha(self, dd, flags, inv_tau, lid_u, g=(0.0, 0.0, 0.0), origin=None, size=None):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        origin = (0, 0, 0) if origin is None else origin
+        size = (nx + 2, ny + 2, nz + 2) if size is None else size
+        R = self._real(dd.dtype)
+        fn = self._fn("alpha", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, R, R, R, R, R, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, g[0], g[1], g[2], lid_u, _i3(origin), _i3(size))
+
+    def beta(self, dd, flags, inv_tau, lid_u, origin=None, size=None):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        origin = (0, 0, 0) if origin is None else origin
+        size = (nx + 2, ny + 2, nz + 2) if size is None else size
+        R = self._real(dd.dtype)
+        fn = self._fn("beta", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, R, R, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, _i3(origin), _i3(size))
+
+    def macros(self, dd, flags, last_was_alpha, lid_u):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        out = [np.zeros(flags.shape, dtype=dd.dtype) for _ in range(4)]
+        R = self._real(dd.dtype)
+        fn = self._fn("macros", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, _I, R, _P, _P, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, int(bool(last_was_alpha)), lid_u, *[_ptr(o) for o in out])
+        return out  # rho, jx, jy, jz
+
+    def reduce(self, dd, flags, last_was_alpha):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        out = np.zeros(4, dtype=np.float64)
+        fn = self._fn("reduce", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, _I, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, int(bool(last_was_alpha)), _ptr(out))
+        return out  # mass, px, py, pz
+
+    # -- convenience: the reference's time loop (src/CController.cpp:1278-1287) --
+    def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):
+        if counter & 1:
+            self.beta(dd, flags, inv_tau, lid_u)
+        else:
+            self.alpha(dd, flags, inv_tau, lid_u, g)
+
+    def run_cavity(self, nx, ny, nz, dtype, inv_tau, lid_u, steps, g=(0.0, 0.0, 0.0), lid=True):
+        dd, flags = self.init(nx, ny, nz, dtype)
+        if lid:
+            self.set_lid(flags)
+        for i in range(steps):
+            self.step(dd, flags, i, inv_tau, lid_u, g)
+        return dd, flags
+
+
+class Reference(_Lib):
+    """The reference's own CPU kernels (oracle/_ref/libref_cavity.so)."""
+
+    prefix = "ref"
+
+    def __init__(self, path: str = REF_SO):
+        super().__init__(path)
+
+    def alpha(self, dd, flags, inv_tau, lid_u, g=(0.0, 0.0, 0.0), origin=None, size=None, block=(32, 32, 32)):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        origin = (0, 0, 0) if origin is None else origin
+        size = (nx + 2, ny + 2, nz + 2) if size is None else size
+        R = self._real(dd.dtype)
+        fn = self._fn("alpha", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, R, R, R, R, R, _P, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, g[0], g[1], g[2], lid_u,
+           _i3(origin), _i3(size), _i3(block))
+
+    def beta(self, dd, flags, inv_tau, lid_u, origin=None, size=None, block=(32, 32, 32)):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        origin = (0, 0, 0) if origin is None else origin
+        size = (nx + 2, ny + 2, nz + 2) if size is None else size
+        R = self._real(dd.dtype)
+        fn = self._fn("beta", dd.dtype)
+        fn.argtypes = [_P, _P, _I, _I, _I, R, R, _P, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, _i3(origin), _i3(size), _i3(block))
+
+    def params(self, xml_path: str, dtype) -> np.ndarray:
+        """(timestep, tau, tauInv, U*x, U*y, U*z, g*x, g*y, g*z, nu*) as the
+        reference's CLbmSolver constructor derives them (src/CLbmSolver.cpp:28-327)."""
+        out = np.zeros(10, dtype=np.float64)
+        fn = self._fn("params", dtype)
+        fn.argtypes = [C.c_char_p, _P]
+        fn(xml_path.encode(), _ptr(out))
+        return out
+
+    def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):
+        if counter & 1:
+            self.beta(dd, flags, inv_tau, lid_u)
+        else:
+            self.alpha(dd, flags, inv_tau, lid_u, g)
+
+    def run_cavity(self, nx, ny, nz, dtype, inv_tau, lid_u, steps, g=(0.0, 0.0, 0.0), lid=True):
+        dd, flags = self.init(nx, ny, nz, dtype)
+        if lid:
+            flags[1:-1, ny, 1:-1] = VELOCITY_INJECTION  # src/CController.cpp:1313-1345
+        for i in range(steps):
+            self.step(dd, flags, i, inv_tau, lid_u, g)
+        return dd, flags
+
+
+def tau_of(nu, dtype):
+    """tau = 0.5*(6 nu + 1) and 1/tau in the working precision, for dx = dt = 1
+    (src/CLbmSolver.cpp:227, :281)."""
+    T = np.dtype(dtype).type
+    tau = T(0.5) * (T(6) * T(nu) + T(1))
+    return tau, T(1) / tau

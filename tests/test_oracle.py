@@ -1,0 +1,127 @@
+"""The CPU oracle pinned against the reference's own kernels (CPU only).
+
+Golden fixtures in tests/golden were produced by running the reference's CPU
+kernels (src/cpukernels/CLbm{Init,Alpha,Beta}CPU.cpp) built from its sources;
+see tests/golden/make_golden.py.  The oracle must reproduce them bit for bit.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle import oracle as orc
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+SMALL = ["cube8_f64", "box10x7x5_f64", "cube8_f32", "box13x6x9_f32", "gravity12x9x6_f32", "gravity9x9x9_f64",
+         "walls10_f64"]
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_oracle_matches_reference_fixtures(oracle, name):
+    z = _load(name)
+    dtype = z["init_dd"].dtype
+    nx, ny, nz = int(z["nx"]), int(z["ny"]), int(z["nz"])
+    dd, flags = oracle.init(nx, ny, nz, dtype)
+    assert np.array_equal(dd, z["init_dd"])
+    if bool(z["lid"]):
+        oracle.set_lid(flags)
+    assert np.array_equal(flags, z["flags"])
+    itau, lid_u, g = dtype.type(z["inv_tau"]), dtype.type(z["lid_u"]), tuple(dtype.type(v) for v in z["gravity"])
+    done = 0
+    for n in z["steps"]:
+        while done < n:
+            oracle.step(dd, flags, done, itau, lid_u, g)
+            done += 1
+        assert np.array_equal(dd.view(np.uint8), z[f"dd_{n}"].view(np.uint8)), f"{name} after {n} steps"
+
+
+@pytest.mark.parametrize("tag", ["f64", "f32"])
+def test_oracle_cuboid_steps_and_obstacles(oracle, tag):
+    z = _load(f"cuboid_obstacle_{tag}")
+    dtype = z["dd_final"].dtype
+    nx, ny, nz = int(z["nx"]), int(z["ny"]), int(z["nz"])
+    dd, _ = oracle.init(nx, ny, nz, dtype)
+    flags = z["flags"].copy()
+    itau, lid_u = dtype.type(z["inv_tau"]), dtype.type(z["lid_u"])
+    for kind, o, s in zip(z["seq_kind"], z["seq_origin"], z["seq_size"]):
+        if kind:
+            oracle.beta(dd, flags, itau, lid_u, origin=o, size=s)
+        else:
+            oracle.alpha(dd, flags, itau, lid_u, origin=o, size=s)
+    assert np.array_equal(dd.view(np.uint8), z["dd_final"].view(np.uint8))
+
+
+DIGESTS = json.load(open(os.path.join(GOLDEN, "digests.json")))
+
+
+@pytest.mark.parametrize("name", sorted(DIGESTS))
+def test_oracle_matches_reference_digests(oracle, name):
+    d = DIGESTS[name]
+    dtype = np.dtype(d["dtype"]).type
+    dd, _ = oracle.run_cavity(d["nx"], d["ny"], d["nz"], dtype, dtype(d["inv_tau"]), dtype(d["lid_u"]), d["steps"])
+    assert hashlib.sha256(dd.tobytes()).hexdigest() == d["sha256"]
+
+
+def test_oracle_matches_live_reference(oracle, reference):
+    """Random-ish cases against the reference kernels run now (skipped off this host)."""
+    rng = np.random.default_rng(7)
+    for dtype in (np.float64, np.float32):
+        for _ in range(3):
+            nx, ny, nz = (int(v) for v in rng.integers(3, 14, size=3))
+            nu = float(rng.uniform(0.005, 0.2))
+            U = dtype(rng.uniform(0.0, 0.1))
+            _, itau = orc.tau_of(nu, dtype)
+            steps = int(rng.integers(1, 30))
+            a, _ = oracle.run_cavity(nx, ny, nz, dtype, itau, U, steps)
+            b, _ = reference.run_cavity(nx, ny, nz, dtype, itau, U, steps)
+            assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), (dtype, nx, ny, nz, steps)
+
+
+def test_initial_state_is_rest_equilibrium(oracle):
+    dd, flags = oracle.init(5, 4, 3, np.float64)
+    w = np.array([1 / 18] * 4 + [1 / 36] * 12 + [1 / 18] * 2 + [1 / 3])
+    assert np.array_equal(dd[:, 0, 0, 0], w)
+    assert (flags[1:-1, 1:-1, 1:-1] == orc.FLUID).all()
+    assert (flags[0] == orc.OBSTACLE).all() and (flags[:, :, -1] == orc.OBSTACLE).all()
+
+
+def test_walls_only_conserve_mass(oracle):
+    """Bounce-back on all six walls conserves the live mass to round-off
+    (populations that enter a wall cell's slot wait there one step)."""
+    _, itau = orc.tau_of(0.05, np.float64)
+    dd, flags = oracle.init(12, 10, 9, np.float64)
+    # a non-uniform start so that the walls do work
+    rng = np.random.default_rng(0)
+    dd *= 1 + 0.01 * rng.standard_normal(dd.shape)
+    m0 = oracle.reduce(dd, flags, last_was_alpha=False)[0]
+    for i in range(50):
+        oracle.step(dd, flags, i, itau, 0.0)
+        m = oracle.reduce(dd, flags, last_was_alpha=bool(i % 2 == 0))[0]
+        assert abs(m - m0) <= 1e-13 * m0
+
+
+def test_lid_changes_mass(oracle):
+    _, itau = orc.tau_of(0.032, np.float64)
+    dd, flags = oracle.init(10, 10, 10, np.float64)
+    oracle.set_lid(flags)
+    m0 = oracle.reduce(dd, flags, last_was_alpha=False)[0]
+    for i in range(40):
+        oracle.step(dd, flags, i, itau, 0.1)
+    assert abs(oracle.reduce(dd, flags, last_was_alpha=True)[0] - m0) > 1e-9 * m0
+
+
+def test_macros_of_lid_and_walls(oracle):
+    _, itau = orc.tau_of(0.032, np.float64)
+    dd, flags = oracle.run_cavity(6, 5, 4, np.float64, itau, 0.07, 9)
+    rho, jx, jy, jz = oracle.macros(dd, flags, last_was_alpha=True, lid_u=0.07)
+    assert (rho[:, 5, 1:-1][1:-1] == 1.0).all() and (jx[1:-1, 5, 1:-1] == 0.07).all()
+    assert (rho[0] == 0).all() and (jx[:, 0] == 0).all()
+    # interior fluid: sums of post-collision populations
+    assert np.all(np.abs(rho[1:-1, 1:-2, 1:-1] - 1.0) < 0.05)
