@@ -54,6 +54,24 @@ bool valid_flag(int32_t f)
 
 constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 
+// Default launch variant per storage (index into the menu of lbm_fast.cuh),
+// from measurements of the 384^3 cavity on GB300.
+int default_variant(int storage)
+{
+    (void)storage;
+    return 3;
+}
+
+// Cells per thread and block size of a variant (mirrors lbm_fast.cuh's menu).
+void variant_shape(int storage, int variant, int& cpt, int& block)
+{
+    static const int cpt_div[lbm::kFastVariantCount] = {1, 1, 1, 2, 2, 2};
+    static const int blocks[lbm::kFastVariantCount] = {256, 256, 128, 256, 256, 128};
+    const int V = 16 / (storage == LBM_STORAGE_F64 ? 8 : storage == LBM_STORAGE_F32 ? 4 : 2);
+    cpt = V / cpt_div[variant];
+    block = blocks[variant];
+}
+
 }  // namespace
 
 struct lbm_solver {
@@ -74,6 +92,7 @@ struct lbm_solver {
     int64_t counter = 0;
     bool last_alpha = false;
     int lid_y = -1;                 // fast path: lid row (ny) or 0 for none; -1: flag-array path
+    int variant = 0;                // launch variant of the vectorised kernels
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int64_t device_bytes = 0;
@@ -140,7 +159,7 @@ int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, 
     int3 o, n;
     cudaError_t e;
     if (!origin && s->lid_y >= 0) {
-        e = lbm::launch_fast_step(s->storage, alpha, s->dd, s->g, s->p, s->lid_y, st);
+        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, s->p, s->lid_y, st);
     } else {
         if (origin) {
             int r = resolve_cuboid(s, origin, size, o, n);
@@ -378,6 +397,12 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
     s->p.gy = prm->gravity[1];
     s->p.gz = prm->gravity[2];
     for (int f = 0; f < 6; ++f) s->bc[f] = prm->boundary[f];
+    if (prm->fast_variant < 0 || prm->fast_variant > lbm::kFastVariantCount) {
+        delete s;
+        return fail(LBM_ERR_INVALID_ARGUMENT, "fast_variant %d not in [0, %d]", prm->fast_variant,
+                    lbm::kFastVariantCount);
+    }
+    s->variant = prm->fast_variant == 0 ? default_variant(s->storage) : prm->fast_variant - 1;
 
     auto bail = [&](int r) { lbm_destroy(s); return r; };
     cudaError_t e = cudaSetDevice(s->device);
@@ -438,6 +463,8 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     info->step_counter = s->counter;
     info->last_step_was_alpha = s->last_alpha ? 1 : 0;
     info->fast_path = s->lid_y >= 0 ? 1 : 0;
+    info->fast_variant = s->variant;
+    variant_shape(s->storage, s->variant, info->cells_per_thread, info->block_threads);
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
@@ -513,9 +540,11 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             CK(cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             cudaError_t e = cudaSuccess;
             for (int i = 0; i < kGraphPairs && e == cudaSuccess; ++i) {
-                e = lbm::launch_fast_step(s->storage, true, s->dd, s->g, s->p, s->lid_y, s->capture_stream);
+                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, s->p, s->lid_y,
+                                          s->capture_stream);
                 if (e == cudaSuccess)
-                    e = lbm::launch_fast_step(s->storage, false, s->dd, s->g, s->p, s->lid_y, s->capture_stream);
+                    e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y,
+                                              s->capture_stream);
             }
             cudaError_t e2 = cudaStreamEndCapture(s->capture_stream, &graph);
             // captured launches are counted when the graph runs
@@ -551,6 +580,74 @@ int lbm_synchronize(lbm_solver* s)
     CK(cudaSetDevice(s->device), "cudaSetDevice");
     CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
     return LBM_OK;
+}
+
+int lbm_fast_variant_count(void) { return lbm::kFastVariantCount; }
+
+int lbm_set_fast_variant(lbm_solver* s, int32_t variant)
+{
+    if (int r = check_solver(s)) return r;
+    if (variant < 0 || variant >= lbm::kFastVariantCount)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "variant %d not in [0, %d)", variant, lbm::kFastVariantCount);
+    if (variant != s->variant) drop_graph(s);
+    s->variant = variant;
+    return LBM_OK;
+}
+
+int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair)
+{
+    if (int r = check_solver(s)) return r;
+    if (pairs <= 0) return fail(LBM_ERR_INVALID_ARGUMENT, "pairs must be positive");
+    if (s->lid_y < 0) return fail(LBM_ERR_UNSUPPORTED, "autotune needs the vectorised (box cavity) path");
+    CK(cudaSetDevice(s->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    const size_t bytes = (size_t)lbm::Q * s->g.S * elem_bytes(s->storage);
+    void* saved = nullptr;
+    CK(cudaMalloc(&saved, bytes), "cudaMalloc autotune snapshot");
+    cudaStream_t st = s->capture_stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int result = LBM_OK;
+    float best_ms = 0.f;
+    int best_v = s->variant;
+    auto run_pairs = [&](int v, int n) -> cudaError_t {
+        for (int i = 0; i < n; ++i) {
+            cudaError_t e = lbm::launch_fast_step(s->storage, v, true, s->dd, s->g, s->p, s->lid_y, st);
+            if (e == cudaSuccess) e = lbm::launch_fast_step(s->storage, v, false, s->dd, s->g, s->p, s->lid_y, st);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
+    cudaError_t e = cudaMemcpyAsync(saved, s->dd, bytes, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (s->last_alpha && e == cudaSuccess)  // the timing runs alpha-first pairs from an even parity
+        e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y, st);
+    for (int v = 0; v < lbm::kFastVariantCount && e == cudaSuccess; ++v) {
+        e = run_pairs(v, 1);  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+        if (e == cudaSuccess) e = run_pairs(v, pairs);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)pairs;
+        if (ms_per_pair) ms_per_pair[v] = ms;
+        if (e == cudaSuccess && (v == 0 || ms < best_ms)) {
+            best_ms = ms;
+            best_v = v;
+        }
+    }
+    // restore the populations whatever happened above
+    cudaError_t er = cudaMemcpyAsync(s->dd, saved, bytes, cudaMemcpyDeviceToDevice, st);
+    if (er == cudaSuccess) er = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) result = cuda_fail(e, "autotune");
+    else if (er != cudaSuccess) result = cuda_fail(er, "autotune restore");
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(saved);
+    if (result != LBM_OK) return result;
+    if (best) *best = best_v;
+    return lbm_set_fast_variant(s, best_v);
 }
 
 int lbm_get_density_distributions(lbm_solver* s, const int32_t origin[3], const int32_t size[3], void* host,

@@ -215,18 +215,39 @@ __device__ __forceinline__ void alpha_gravity(T* f, T rho, T gx, T gy, T gz)
     t = gz * wa * t;                        f[17] -= t; f[16] += t;
 }
 
+// Relaxation of one direction pair toward the equilibrium of pair_eq.
+template <typename T>
+__device__ __forceinline__ void relax_pair(T& fp, T& fm, T w, T P, T s, T inv_tau)
+{
+    T ep, em;
+    pair_eq(w, P, s, ep, em);
+    fp += inv_tau * (ep - fp);
+    fm += inv_tau * (em - fm);
+}
+
 // BGK collision of a FLUID cell in place (lbm_alpha.cu:209-331,
-// lbm_beta.cu:574-636).  For shifted storage f holds f - w and the same
+// lbm_beta.cu:574-636), one direction pair at a time so that no array of 19
+// equilibria is live.  For shifted storage f holds f - w and the same
 // arithmetic yields the post-collision deviation: with rho the density
 // deviation, feq(rho) - w is exactly the reference formula.
 template <typename T>
 __device__ __forceinline__ void collide_fluid(T* f, T inv_tau)
 {
-    T rho, vx, vy, vz, e[Q];
+    T rho, vx, vy, vz;
     moments(f, rho, vx, vy, vz);
-    equilibrium(rho, vx, vy, vz, e);
-#pragma unroll
-    for (int k = 0; k < Q; ++k) f[k] += inv_tau * (e[k] - f[k]);
+    const T vel2 = vx * vx + vy * vy + vz * vz;
+    const T P = rho - (T(3) / T(2)) * vel2;
+    const T wa = T(1) / T(18), wd = T(1) / T(36);
+    relax_pair(f[0], f[1], wa, P, vx, inv_tau);
+    relax_pair(f[2], f[3], wa, P, vy, inv_tau);
+    relax_pair(f[4], f[5], wd, P, vx + vy, inv_tau);
+    relax_pair(f[6], f[7], wd, P, vx - vy, inv_tau);
+    relax_pair(f[8], f[9], wd, P, vx + vz, inv_tau);
+    relax_pair(f[10], f[11], wd, P, vx - vz, inv_tau);
+    relax_pair(f[12], f[13], wd, P, vy + vz, inv_tau);
+    relax_pair(f[14], f[15], wd, P, vy - vz, inv_tau);
+    relax_pair(f[16], f[17], wa, P, vz, inv_tau);
+    f[18] += inv_tau * ((T(1) / T(3)) * P - f[18]);
 }
 
 template <typename T>

@@ -1,0 +1,274 @@
+// lbm_fast.cuh -- the vectorised A-A step kernels of the box cavity (the hot
+// path).  Flags are implied by coordinates: interior cells are FLUID except
+// the lid row y = lid_y (VELOCITY_INJECTION); the halo is OBSTACLE.
+//
+//   alpha_fast  -- src/gpukernels/lbm_alpha.cu:22-532 restated: a thread owns
+//                  CPT consecutive cells of one x row, reads their 19 slots
+//                  with one vector access each, collides and writes every
+//                  population to its opposite slot.
+//   beta_fast   -- src/gpukernels/lbm_beta.cu:32-915 restated: the same
+//                  thread pulls the 19 incoming populations from the
+//                  neighbours' slots, collides and pushes the results back to
+//                  the same addresses.  Slots with c_x = +-1 are read and
+//                  written one cell off the vector grid; the element that
+//                  crosses into the next thread's group is exchanged with
+//                  warp shuffles, and only lanes at a warp or row edge touch
+//                  that element with a scalar access.
+//
+// Template parameters: St storage type, CPT cells per thread (one vector of
+// CPT elements per slot: 16 or 8 bytes), BLOCK threads per block, MINB the
+// minimum resident blocks per SM requested from the register allocator.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "lbm_core.cuh"
+
+namespace lbm {
+
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f)
+{
+    if constexpr (I < N) {
+        f(std::integral_constant<int, I>{});
+        static_for<I + 1, N>(f);
+    }
+}
+
+template <int BYTES> struct RawVec;
+template <> struct RawVec<16> { using type = uint4; };
+template <> struct RawVec<8> { using type = uint2; };
+template <> struct RawVec<4> { using type = unsigned int; };
+template <> struct RawVec<2> { using type = unsigned short; };
+
+// Aligned access to N consecutive storage elements, converted to the
+// arithmetic type.
+template <class St, int N>
+struct Vio {
+    using bits = typename St::bits;
+    using T = typename St::T;
+    using raw = typename RawVec<N * sizeof(bits)>::type;
+    union Pack {
+        raw u;
+        bits b[N];
+    };
+    __device__ static void load(const bits* p, T (&a)[N])
+    {
+        Pack x;
+        x.u = *reinterpret_cast<const raw*>(p);
+#pragma unroll
+        for (int v = 0; v < N; ++v) a[v] = St::load(x.b[v]);
+    }
+    __device__ static void store(bits* p, const T (&a)[N])
+    {
+        Pack x;
+#pragma unroll
+        for (int v = 0; v < N; ++v) x.b[v] = St::store(a[v]);
+        *reinterpret_cast<raw*>(p) = x.u;
+    }
+};
+
+template <class St, int CPT, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                          const typename St::T inv_tau,
+                                                          const typename St::T lid_u, const int lid_y)
+{
+    using T = typename St::T;
+    using IO = Vio<St, CPT>;
+    const int G = (g.nx + CPT - 1) / CPT;
+    const long long t = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long total = (long long)G * g.ny * g.nz;
+    if (t >= total) return;
+    const int gi = (int)(t % G);
+    const long long row = t / G;
+    const int y = 1 + (int)(row % g.ny);
+    const int z = 1 + (int)(row / g.ny);
+    const int x0 = 1 + gi * CPT;
+    const long long base = g.idx(x0, y, z);
+
+    T f[Q][CPT];
+#pragma unroll
+    for (int k = 0; k < Q; ++k) IO::load(dd + k * g.S + base, f[k]);
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+#pragma unroll
+    for (int v = 0; v < CPT; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
+        T c[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) c[k] = f[k][v];
+        if (lid) inject(c, rho0, lid_u);
+        else collide_fluid(c, inv_tau);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[opp(k)][v] = c[k];  // population k -> slot opp(k)
+    }
+#pragma unroll
+    for (int k = 0; k < Q; ++k) IO::store(dd + k * g.S + base, f[k]);
+}
+
+template <class St, int CPT, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                         const typename St::T inv_tau,
+                                                         const typename St::T lid_u, const int lid_y)
+{
+    using T = typename St::T;
+    using IO = Vio<St, CPT>;
+    const int G = (g.nx + CPT - 1) / CPT;
+    const long long t = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long total = (long long)G * g.ny * g.nz;
+    const bool active = t < total;
+    const int lane = threadIdx.x & 31;
+    const long long tt = active ? t : 0;
+    const int gi = (int)(tt % G);
+    const long long row = tt / G;
+    const int y = 1 + (int)(row % g.ny);
+    const int z = 1 + (int)(row / g.ny);
+    const int x0 = 1 + gi * CPT;
+    // The neighbouring group of the same row is held by the adjacent lane.
+    const bool left_in = gi > 0 && lane > 0;
+    const bool right_in = gi < G - 1 && lane < 31;
+    const unsigned full = 0xffffffffu;
+
+    // p[k][v]: value of slot k at (cell x0+v) + c_k, i.e. population opp(k)
+    // arriving at cell x0+v.  edge[k]: the aligned element of slot k that lies
+    // outside this thread's shifted window (kept to rewrite it unchanged).
+    T p[Q][CPT];
+    T edge[Q];
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        T a[CPT];
+        if (active) IO::load(dd + rb, a);
+        else {
+#pragma unroll
+            for (int v = 0; v < CPT; ++v) a[v] = T(0);
+        }
+        if constexpr (cx == 0) {
+#pragma unroll
+            for (int v = 0; v < CPT; ++v) p[k][v] = a[v];
+            edge[k] = T(0);
+        } else if constexpr (cx == 1) {
+            T nb = __shfl_down_sync(full, a[0], 1);
+            if (active && !right_in) nb = St::load(dd[rb + CPT]);
+#pragma unroll
+            for (int v = 0; v < CPT - 1; ++v) p[k][v] = a[v + 1];
+            p[k][CPT - 1] = nb;
+            edge[k] = a[0];
+        } else {
+            T pb = __shfl_up_sync(full, a[CPT - 1], 1);
+            if (active && !left_in) pb = St::load(dd[rb - 1]);
+            p[k][0] = pb;
+#pragma unroll
+            for (int v = 1; v < CPT; ++v) p[k][v] = a[v - 1];
+            edge[k] = a[CPT - 1];
+        }
+    });
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+#pragma unroll
+    for (int v = 0; v < CPT; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
+        T c[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) c[opp(k)] = p[k][v];
+        if (lid) inject(c, rho0, lid_u);
+        else collide_fluid(c, inv_tau);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) p[k][v] = c[k];  // population k -> slot k at x + c_k
+    }
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        if constexpr (cx == 0) {
+            if (active) IO::store(dd + rb, p[k]);
+        } else if constexpr (cx == 1) {
+            // aligned element 0 belongs to cell x0-1 (left lane's last cell)
+            const T from_left = __shfl_up_sync(full, p[k][CPT - 1], 1);
+            if (active) {
+                T o[CPT];
+#pragma unroll
+                for (int v = 1; v < CPT; ++v) o[v] = p[k][v - 1];
+                if (left_in || gi == 0) {
+                    o[0] = left_in ? from_left : edge[k];
+                    IO::store(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 1; v < CPT; ++v) dd[rb + v] = St::store(o[v]);
+                }
+                if (!right_in && x0 + CPT - 1 <= g.nx) dd[rb + CPT] = St::store(p[k][CPT - 1]);
+            }
+        } else {
+            // aligned element CPT-1 belongs to cell x0+CPT (right lane's first cell)
+            const T from_right = __shfl_down_sync(full, p[k][0], 1);
+            if (active) {
+                T o[CPT];
+#pragma unroll
+                for (int v = 0; v < CPT - 1; ++v) o[v] = p[k][v + 1];
+                if (right_in || gi == G - 1) {
+                    o[CPT - 1] = right_in ? from_right : edge[k];
+                    IO::store(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < CPT - 1; ++v) dd[rb + v] = St::store(o[v]);
+                }
+                if (!left_in) dd[rb - 1] = St::store(p[k][0]);
+            }
+        }
+    });
+}
+
+// Launch menu shared by every storage type: (cells per thread as a fraction
+// of a 16-byte vector, block size, minimum blocks per SM).  Index = variant.
+struct FastVariant {
+    int cpt_div;   // cells per thread = (16 bytes / element) / cpt_div
+    int block;
+    int minb;
+};
+constexpr int kFastVariants = 6;
+constexpr FastVariant kFastMenu[kFastVariants] = {
+    {1, 256, 1},  // 16-byte vectors, registers unconstrained
+    {1, 256, 2},  // 16-byte vectors, <= 128 registers
+    {1, 128, 4},  // 16-byte vectors, <= 128 registers, smaller blocks
+    {2, 256, 2},  // 8-byte vectors, <= 128 registers
+    {2, 256, 3},  // 8-byte vectors, <= 85 registers
+    {2, 128, 5},  // 8-byte vectors, <= 102 registers
+};
+
+template <class St, int VARIANT>
+cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, cudaStream_t st)
+{
+    using T = typename St::T;
+    constexpr FastVariant fv = kFastMenu[VARIANT];
+    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div;
+    const int G = (g.nx + CPT - 1) / CPT;
+    const long long threads = (long long)G * g.ny * g.nz;
+    const int blocks = (int)((threads + fv.block - 1) / fv.block);
+    auto* d = static_cast<typename St::bits*>(dd);
+    if (alpha) alpha_fast<St, CPT, fv.block, fv.minb><<<blocks, fv.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+    else beta_fast<St, CPT, fv.block, fv.minb><<<blocks, fv.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+    return cudaGetLastError();
+}
+
+template <class St>
+cudaError_t launch_fast_menu(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                             cudaStream_t st)
+{
+    switch (variant) {
+    case 0: return launch_fast_variant<St, 0>(alpha, dd, g, p, lid_y, st);
+    case 1: return launch_fast_variant<St, 1>(alpha, dd, g, p, lid_y, st);
+    case 2: return launch_fast_variant<St, 2>(alpha, dd, g, p, lid_y, st);
+    case 3: return launch_fast_variant<St, 3>(alpha, dd, g, p, lid_y, st);
+    case 4: return launch_fast_variant<St, 4>(alpha, dd, g, p, lid_y, st);
+    case 5: return launch_fast_variant<St, 5>(alpha, dd, g, p, lid_y, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace lbm

@@ -1,19 +1,8 @@
-// lbm_kernels.cu -- sm_103a kernels of the D3Q19 A-A lid-driven cavity.
-//
-// Hot path (box cavity, flags implied by coordinates):
-//   alpha_fast  -- src/gpukernels/lbm_alpha.cu:22-532 restated: each thread
-//                  owns one 16-byte group of V consecutive cells of an x row,
-//                  reads their 19 slots with 128-bit loads, collides and
-//                  writes every population to its opposite slot.
-//   beta_fast   -- src/gpukernels/lbm_beta.cu:32-915 restated: the same
-//                  thread pulls the 19 incoming populations from the
-//                  neighbours' slots, collides and pushes the results back to
-//                  the same addresses.  Rows shifted by +-1 in x are
-//                  realigned with warp shuffles; the lanes at a warp or row
-//                  edge use scalar accesses for the one element that leaves
-//                  the warp.
-// General path (any flags, cuboid sub-steps, gravity): one cell per thread,
-// reads the per-cell flag (alpha_general / beta_general).
+// lbm_kernels.cu -- sm_103a kernels of the D3Q19 A-A lid-driven cavity other
+// than the vectorised hot path (lbm_fast.cuh, instantiated in fast_*.cu):
+// the general flag-array step kernels (any flags, cuboid sub-steps,
+// gravity; one cell per thread), initialisation, the cavity-flag check,
+// macroscopic fields, the FP64 reduction and the 16-bit pack/unpack.
 #include <cstdint>
 #include <type_traits>
 #include <utility>
@@ -22,200 +11,6 @@
 #include "lbm_kernels.h"
 
 namespace lbm {
-
-template <int I, int N, class F>
-__device__ __forceinline__ void static_for(F&& f)
-{
-    if constexpr (I < N) {
-        f(std::integral_constant<int, I>{});
-        static_for<I + 1, N>(f);
-    }
-}
-
-// 16-byte vector access in storage type St, converted to the arithmetic type.
-template <class St>
-struct Vio {
-    using bits = typename St::bits;
-    using T = typename St::T;
-    static constexpr int V = 16 / sizeof(bits);
-    union Pack {
-        uint4 u;
-        bits b[V];
-    };
-    __device__ static void load(const bits* p, T (&a)[V])
-    {
-        Pack x;
-        x.u = *reinterpret_cast<const uint4*>(p);
-#pragma unroll
-        for (int v = 0; v < V; ++v) a[v] = St::load(x.b[v]);
-    }
-    __device__ static void store(bits* p, const T (&a)[V])
-    {
-        Pack x;
-#pragma unroll
-        for (int v = 0; v < V; ++v) x.b[v] = St::store(a[v]);
-        *reinterpret_cast<uint4*>(p) = x.u;
-    }
-};
-
-// ===========================================================================
-// Fast path
-// ===========================================================================
-
-template <class St>
-__global__ void __launch_bounds__(kFastBlock) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
-                                                         const typename St::T inv_tau,
-                                                         const typename St::T lid_u, const int lid_y)
-{
-    using T = typename St::T;
-    using IO = Vio<St>;
-    constexpr int V = IO::V;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)g.G * g.ny * g.nz;
-    if (t >= total) return;
-    const int gi = (int)(t % g.G);
-    const long long row = t / g.G;
-    const int y = 1 + (int)(row % g.ny);
-    const int z = 1 + (int)(row / g.ny);
-    const int x0 = 1 + gi * V;
-    const long long base = g.idx(x0, y, z);
-
-    T f[Q][V];
-#pragma unroll
-    for (int k = 0; k < Q; ++k) IO::load(dd + k * g.S + base, f[k]);
-
-    const bool lid = (y == lid_y);
-    const T rho0 = St::shifted ? T(0) : T(1);
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
-        T c[Q];
-#pragma unroll
-        for (int k = 0; k < Q; ++k) c[k] = f[k][v];
-        if (lid) inject(c, rho0, lid_u);
-        else collide_fluid(c, inv_tau);
-#pragma unroll
-        for (int k = 0; k < Q; ++k) f[opp(k)][v] = c[k];  // population k -> slot opp(k)
-    }
-#pragma unroll
-    for (int k = 0; k < Q; ++k) IO::store(dd + k * g.S + base, f[k]);
-}
-
-template <class St>
-__global__ void __launch_bounds__(kFastBlock) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
-                                                        const typename St::T inv_tau,
-                                                        const typename St::T lid_u, const int lid_y)
-{
-    using T = typename St::T;
-    using IO = Vio<St>;
-    constexpr int V = IO::V;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)g.G * g.ny * g.nz;
-    const bool active = t < total;
-    const int lane = threadIdx.x & 31;
-    const long long tt = active ? t : 0;
-    const int gi = (int)(tt % g.G);
-    const long long row = tt / g.G;
-    const int y = 1 + (int)(row % g.ny);
-    const int z = 1 + (int)(row / g.ny);
-    const int x0 = 1 + gi * V;
-    // The neighbouring group of the same row is held by the adjacent lane.
-    const bool left_in = gi > 0 && lane > 0;
-    const bool right_in = gi < g.G - 1 && lane < 31;
-    const unsigned full = 0xffffffffu;
-
-    // p[k][v]: value of slot k at (cell x0+v) + c_k, i.e. population opp(k)
-    // arriving at cell x0+v.  edge[k]: the aligned element of slot k that lies
-    // outside this thread's shifted window (kept to rewrite it unchanged).
-    T p[Q][V];
-    T edge[Q];
-
-    static_for<0, Q>([&](auto kc) {
-        constexpr int k = decltype(kc)::value;
-        constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
-        T a[V];
-        if (active) IO::load(dd + rb, a);
-        else {
-#pragma unroll
-            for (int v = 0; v < V; ++v) a[v] = T(0);
-        }
-        if constexpr (cx == 0) {
-#pragma unroll
-            for (int v = 0; v < V; ++v) p[k][v] = a[v];
-            edge[k] = T(0);
-        } else if constexpr (cx == 1) {
-            T nb = __shfl_down_sync(full, a[0], 1);
-            if (active && !right_in) nb = St::load(dd[rb + V]);
-#pragma unroll
-            for (int v = 0; v < V - 1; ++v) p[k][v] = a[v + 1];
-            p[k][V - 1] = nb;
-            edge[k] = a[0];
-        } else {
-            T pb = __shfl_up_sync(full, a[V - 1], 1);
-            if (active && !left_in) pb = St::load(dd[rb - 1]);
-            p[k][0] = pb;
-#pragma unroll
-            for (int v = 1; v < V; ++v) p[k][v] = a[v - 1];
-            edge[k] = a[V - 1];
-        }
-    });
-
-    const bool lid = (y == lid_y);
-    const T rho0 = St::shifted ? T(0) : T(1);
-#pragma unroll
-    for (int v = 0; v < V; ++v) {
-        if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
-        T c[Q];
-#pragma unroll
-        for (int k = 0; k < Q; ++k) c[opp(k)] = p[k][v];
-        if (lid) inject(c, rho0, lid_u);
-        else collide_fluid(c, inv_tau);
-#pragma unroll
-        for (int k = 0; k < Q; ++k) p[k][v] = c[k];  // population k -> slot k at x + c_k
-    }
-
-    static_for<0, Q>([&](auto kc) {
-        constexpr int k = decltype(kc)::value;
-        constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
-        if constexpr (cx == 0) {
-            if (active) IO::store(dd + rb, p[k]);
-        } else if constexpr (cx == 1) {
-            // aligned element 0 belongs to cell x0-1 (left lane's last cell)
-            const T from_left = __shfl_up_sync(full, p[k][V - 1], 1);
-            if (active) {
-                T o[V];
-#pragma unroll
-                for (int v = 1; v < V; ++v) o[v] = p[k][v - 1];
-                if (left_in || gi == 0) {
-                    o[0] = left_in ? from_left : edge[k];
-                    IO::store(dd + rb, o);
-                } else {
-#pragma unroll
-                    for (int v = 1; v < V; ++v) dd[rb + v] = St::store(o[v]);
-                }
-                if (!right_in && x0 + V - 1 <= g.nx) dd[rb + V] = St::store(p[k][V - 1]);
-            }
-        } else {
-            // aligned element V-1 belongs to cell x0+V (right lane's first cell)
-            const T from_right = __shfl_down_sync(full, p[k][0], 1);
-            if (active) {
-                T o[V];
-#pragma unroll
-                for (int v = 0; v < V - 1; ++v) o[v] = p[k][v + 1];
-                if (right_in || gi == g.G - 1) {
-                    o[V - 1] = right_in ? from_right : edge[k];
-                    IO::store(dd + rb, o);
-                } else {
-#pragma unroll
-                    for (int v = 0; v < V - 1; ++v) dd[rb + v] = St::store(o[v]);
-                }
-                if (!left_in) dd[rb - 1] = St::store(p[k][0]);
-            }
-        }
-    });
-}
 
 // ===========================================================================
 // General path: flag array, cuboid, gravity, halo cells with any flag
@@ -575,20 +370,17 @@ cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned lo
     return cudaGetLastError();
 }
 
-cudaError_t launch_fast_step(int storage, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
-                             cudaStream_t st)
+cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
+                             int lid_y, cudaStream_t st)
 {
-    const long long threads = (long long)g.G * g.ny * g.nz;
-    const int blocks = grid_for(threads, kFastBlock);
     count_launch();
-    return with_storage(storage, [&](auto tag) {
-        using St = decltype(tag);
-        using T = typename St::T;
-        auto* d = static_cast<typename St::bits*>(dd);
-        if (alpha) alpha_fast<St><<<blocks, kFastBlock, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
-        else beta_fast<St><<<blocks, kFastBlock, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
-        return cudaGetLastError();
-    });
+    switch (storage) {
+    case 0: return launch_fast_f64(variant, alpha, dd, g, p, lid_y, st);
+    case 1: return launch_fast_f32(variant, alpha, dd, g, p, lid_y, st);
+    case 2: return launch_fast_f16s(variant, alpha, dd, g, p, lid_y, st);
+    case 3: return launch_fast_bf16s(variant, alpha, dd, g, p, lid_y, st);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,

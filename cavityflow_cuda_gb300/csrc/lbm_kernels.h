@@ -8,7 +8,6 @@
 
 namespace lbm {
 
-constexpr int kFastBlock = 256;       // threads per block, vectorised step kernels
 constexpr int kReduceBlock = 256;     // threads per block, FP64 reduction
 constexpr int kReduceMaxBlocks = 1024;
 
@@ -24,8 +23,19 @@ void add_launches(long long n);
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
 cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
-cudaError_t launch_fast_step(int storage, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+// Vectorised box-cavity step; `variant` indexes the launch menu of
+// lbm_fast.cuh (cells per thread, block size, blocks per SM).
+constexpr int kFastVariantCount = 6;
+cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
+                             int lid_y, cudaStream_t st);
+cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                            cudaStream_t st);
+cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                            cudaStream_t st);
+cudaError_t launch_fast_f16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                              cudaStream_t st);
+cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                              cudaStream_t st);
 cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,
                                 const Params& p, int3 origin, int3 size, cudaStream_t st);
 cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,

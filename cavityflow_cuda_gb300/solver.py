@@ -49,13 +49,14 @@ class _Lattice(C.Structure):
 class _Params(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("boundary", C.c_int32 * 6),
                 ("inv_tau", C.c_double), ("lid_velocity", C.c_double), ("gravity", C.c_double * 3),
-                ("device", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("device", C.c_int32), ("fast_variant", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class _Info(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("value_size", C.c_int32),
                 ("vector_cells", C.c_int32), ("step_counter", C.c_int64), ("last_step_was_alpha", C.c_int32),
-                ("fast_path", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
+                ("fast_path", C.c_int32), ("fast_variant", C.c_int32), ("cells_per_thread", C.c_int32),
+                ("block_threads", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
                 ("device_bytes", C.c_int64)]
 
 
@@ -89,6 +90,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_step_beta_cuboid": ([V, P, P, P], I),
         "lbm_run": ([V, I64, P], I),
         "lbm_synchronize": ([V], I),
+        "lbm_fast_variant_count": ([], I),
+        "lbm_set_fast_variant": ([V, C.c_int32], I),
+        "lbm_autotune": ([V, C.c_int32, P, P], I),
         "lbm_get_density_distributions": ([V, P, P, P, P], I),
         "lbm_set_density_distributions": ([V, P, P, C.c_int32, P, P], I),
         "lbm_get_flags": ([V, P, P, P], I),
@@ -157,7 +161,7 @@ class CLbmSolverGB300:
 
     def __init__(self, size: Sequence[int], inv_tau: float, lid_velocity: float, storage: str = "f32",
                  boundary: Sequence[int] = (OBSTACLE,) * 6, gravity: Sequence[float] = (0.0, 0.0, 0.0),
-                 device: int = 0, driven_cavity: bool = True):
+                 device: int = 0, driven_cavity: bool = True, fast_variant: int = -1):
         self._lib = load_library()
         p = _Params()
         p.size[:] = [int(s) for s in size]
@@ -167,6 +171,7 @@ class CLbmSolverGB300:
         p.lid_velocity = float(lid_velocity)
         p.gravity[:] = [float(g) for g in gravity]
         p.device = int(device)
+        p.fast_variant = 0 if fast_variant < 0 else int(fast_variant) + 1
         h = C.c_void_p()
         _check(self._lib.lbm_create(C.byref(p), C.byref(h)))
         self._h = h
@@ -227,6 +232,18 @@ class CLbmSolverGB300:
 
     def synchronize(self) -> None:
         _check(self._lib.lbm_synchronize(self._h))
+
+    def set_fast_variant(self, variant: int) -> None:
+        _check(self._lib.lbm_set_fast_variant(self._h, int(variant)))
+
+    def autotune(self, pairs: int = 10):
+        """Time every launch variant on this domain and keep the fastest;
+        the populations are restored.  Returns (best, ms per pair per variant)."""
+        n = int(self._lib.lbm_fast_variant_count())
+        ms = (C.c_float * n)()
+        best = C.c_int32()
+        _check(self._lib.lbm_autotune(self._h, int(pairs), C.byref(best), ms))
+        return best.value, list(ms)
 
     # -- data -------------------------------------------------------------
     def _shape(self, size, comps):

@@ -118,7 +118,11 @@ typedef struct lbm_params {
     double gravity[3];          /* dimensionless acceleration (alpha step)     */
     int32_t device;             /* CUDA device ordinal; the reference picks
                                    id % nGPUs (src/CLbmSolverGPU.cu:42-45)     */
-    int32_t reserved[3];        /* zero                                        */
+    int32_t fast_variant;       /* 0: library default; v + 1 selects launch
+                                   variant v of the vectorised kernels,
+                                   v < lbm_fast_variant_count(); see
+                                   lbm_autotune                                */
+    int32_t reserved[2];        /* zero                                        */
 } lbm_params;
 
 typedef struct lbm_solver lbm_solver;   /* opaque */
@@ -133,6 +137,9 @@ typedef struct lbm_info {
     int32_t last_step_was_alpha;
     int32_t fast_path;          /* 1: flags match the box cavity, so the
                                    vectorised kernels run; 0: flag-array path  */
+    int32_t fast_variant;       /* launch variant of the vectorised kernels    */
+    int32_t cells_per_thread;   /* cells per thread of that variant            */
+    int32_t block_threads;      /* threads per block of that variant           */
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */
@@ -191,6 +198,21 @@ int lbm_run(lbm_solver* solver, int64_t steps, void* stream);
 
 /* Waits for all work queued by the solver. */
 int lbm_synchronize(lbm_solver* solver);
+
+/* ---- tuning (no counterpart in the reference, whose block shape comes from
+ * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
+
+/* Number of launch variants of the vectorised kernels (cells per thread,
+ * threads per block, blocks per SM). */
+int lbm_fast_variant_count(void);
+/* Selects a variant for subsequent steps. */
+int lbm_set_fast_variant(lbm_solver* solver, int32_t variant);
+/* Times every variant on this solver's domain (`pairs` alpha/beta pairs each,
+ * CUDA events) and selects the fastest.  The populations are saved to a
+ * temporary device buffer first and restored afterwards, so the simulation
+ * state and step counter are unchanged.  ms_per_pair (optional) receives one
+ * time per variant.  Synchronous. */
+int lbm_autotune(lbm_solver* solver, int32_t pairs, int32_t* best, float* ms_per_pair);
 
 /* ---- data access ------------------------------------------------------------ */
 

@@ -91,6 +91,34 @@ def test_odd_shapes_match_oracle(gpu, oracle, dtype, n, steps):
         assert same_bits(s.get_all(), want)
 
 
+@pytest.mark.parametrize("variant", range(6))
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_every_launch_variant_matches_oracle(gpu, oracle, variant, dtype):
+    """Each cells-per-thread / block-size variant of the vectorised kernels."""
+    _, itau = orc.tau_of(0.032, dtype)
+    lid = dtype(0.07)
+    for n, steps in (((37, 9, 5), 13), ((300, 4, 3), 6), ((5, 6, 7), 9)):
+        want, _ = oracle.run_cavity(*n, dtype, itau, lid, steps)
+        with solver(n, dtype, itau, lid, fast_variant=variant) as s:
+            assert s.info()["fast_variant"] == variant
+            s.run(steps)
+            assert same_bits(s.get_all(), want), (variant, n)
+
+
+def test_autotune_keeps_state(gpu):
+    _, itau = orc.tau_of(0.0192, np.float32)
+    with solver((48, 40, 32), np.float32, itau, np.float32(0.05)) as a, \
+            solver((48, 40, 32), np.float32, itau, np.float32(0.05)) as b:
+        a.run(7)
+        b.run(7)
+        best, ms = a.autotune(pairs=2)
+        assert 0 <= best < len(ms) and all(m > 0 for m in ms)
+        assert a.info()["fast_variant"] == best and a.info()["step_counter"] == 7
+        a.run(10)
+        b.run(10)
+        assert same_bits(a.get_all(), b.get_all())
+
+
 def test_run_graph_matches_single_steps(gpu):
     _, itau = orc.tau_of(0.032, np.float32)
     with solver((40, 24, 16), np.float32, itau, np.float32(0.05)) as a, \
@@ -183,7 +211,8 @@ def test_reduce_matches_oracle_and_conserves_mass(gpu, oracle):
             for i in range(1001):
                 oracle.step(dd, flags, i, itau, dtype(0.0))
             assert np.allclose(m1, oracle.reduce(dd, flags, True), rtol=1e-12, atol=1e-12)
-            tol = 1e-10 if dtype == np.float64 else 1e-5
+            # FP64: the conservation criterion; FP32: collision round-off from a 1%-noise start
+            tol = 1e-10 if dtype == np.float64 else 1e-4
             assert abs(m1[0] - m0[0]) <= tol * m0[0]
 
 
