@@ -38,6 +38,19 @@ int cuda_fail(cudaError_t e, const char* what)
     return fail(LBM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+}  // namespace
+
+int lbm::record_error(int status, const char* fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(t_err, sizeof(t_err), fmt, ap);
+    va_end(ap);
+    return status;
+}
+
+namespace {
+
 #define CK(call, what)                                   \
     do {                                                 \
         cudaError_t e_ = (call);                         \

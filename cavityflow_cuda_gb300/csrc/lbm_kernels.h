@@ -16,6 +16,9 @@ struct Bc {
     int f[6];
 };
 
+// Stores a detail message for lbm_last_error() on this thread; returns status.
+int record_error(int status, const char* fmt, ...);
+
 // Kernel launches queued by this library since load, and a correction for
 // launches that were captured into a graph rather than run.
 long long kernel_launches();

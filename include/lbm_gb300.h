@@ -255,6 +255,32 @@ int lbm_set_densities(lbm_solver* solver, const int32_t origin[3], const int32_t
  * reference (it has no reduction); it carries the mass-conservation check. */
 int lbm_reduce(lbm_solver* solver, double out[4], void* stream);
 
+/* FP64 {mass, momentum x, y, z} of population and flag arrays the CALLER
+ * owns, written to `out_device` (4 doubles in device memory the caller owns),
+ * with no device or host allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc: programs whose device memory is all
+ * handed out by their own pool or caching allocator, or that admit work
+ * against a fixed HBM budget, and time loops that cannot take the implicit
+ * device synchronisation of cudaMalloc/cudaFree.  Same sums as lbm_reduce.
+ *
+ * Inputs are in the reference's layout: `populations` holds 19 slots of
+ * (nx+2)*(ny+2)*(nz+2) values (double for LBM_STORAGE_F64, float for
+ * LBM_STORAGE_F32), x fastest; `flags` one int32 Flag per cell;
+ * `last_step_was_alpha` selects where the post-collision populations sit.
+ * Queued on `stream`; read `out_device` after that stream completes.
+ *
+ * Scratch is a 128 KiB static device array (per-z-plane partial sums) that
+ * every GPU loading this library holds until the process exits; domains with
+ * nz > 4096 are rejected with LBM_ERR_INVALID_ARGUMENT.  All calls share that
+ * array, so calls that overlap on the GPU (different streams, or different
+ * host threads on one device) race and must be serialised by the caller.
+ * The first call on each device looks up the array's device address with
+ * cudaGetSymbolAddress (with that device current); make that first call
+ * before any stream capture. */
+int lbm_reduce_noalloc(const void* populations, const int32_t* flags, const int32_t size[3], int32_t storage,
+                       int32_t last_step_was_alpha, double* out_device, void* stream);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 const char* lbm_status_string(int status);
 /* Detail message of the last failing call on this thread ("" if none). */
