@@ -1,7 +1,9 @@
-// fast_bf16s.cu -- instantiates the vectorised step kernels for BF16S storage
-// (one translation unit per storage type so they compile in parallel).
+// fast_bf16s.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
+// step kernels for BF16S storage (one translation unit per storage type, so
+// they compile in parallel).
 #include "lbm_fast.cuh"
 #include "lbm_kernels.h"
+#include "lbm_tma.cuh"
 
 namespace lbm {
 
@@ -9,6 +11,12 @@ cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, 
                            cudaStream_t st)
 {
     return launch_fast_menu<BF16S>(variant, alpha, dd, g, p, lid_y, st);
+}
+
+cudaError_t launch_tma_bf16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                          int consumer_warps, int* err, cudaStream_t st)
+{
+    return launch_tma_impl<BF16S>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
 }
 
 }  // namespace lbm

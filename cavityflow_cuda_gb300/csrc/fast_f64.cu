@@ -1,7 +1,9 @@
-// fast_f64.cu -- instantiates the vectorised step kernels for F64 storage
-// (one translation unit per storage type so they compile in parallel).
+// fast_f64.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
+// step kernels for F64 storage (one translation unit per storage type, so
+// they compile in parallel).
 #include "lbm_fast.cuh"
 #include "lbm_kernels.h"
+#include "lbm_tma.cuh"
 
 namespace lbm {
 
@@ -9,6 +11,12 @@ cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, co
                            cudaStream_t st)
 {
     return launch_fast_menu<F64>(variant, alpha, dd, g, p, lid_y, st);
+}
+
+cudaError_t launch_tma_f64(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                          int consumer_warps, int* err, cudaStream_t st)
+{
+    return launch_tma_impl<F64>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
 }
 
 }  // namespace lbm

@@ -68,20 +68,28 @@ bool valid_flag(int32_t f)
 constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 
 // Default launch variant per storage (index into the menu of lbm_fast.cuh),
-// from measurements of the 384^3 cavity on GB300.
+// from autotuner measurements of the 384^3 cavity on GB300: 8-byte vectors
+// at two blocks per SM, except BF16, whose conversions favour 16-byte
+// vectors at one block per SM.
 int default_variant(int storage)
 {
-    (void)storage;
-    return 3;
+    return storage == LBM_STORAGE_BF16S ? 0 : 3;
 }
 
-// Cells per thread and block size of a variant (mirrors lbm_fast.cuh's menu).
-void variant_shape(int storage, int variant, int& cpt, int& block)
+// Cells per thread and block size of a variant (mirrors the menus of
+// lbm_fast.cuh and lbm_kernels.h).
+void variant_shape(int storage, int variant, int nx, int& cpt, int& block)
 {
-    static const int cpt_div[lbm::kFastVariantCount] = {1, 1, 1, 2, 2, 2};
-    static const int blocks[lbm::kFastVariantCount] = {256, 256, 128, 256, 256, 128};
+    static const int cpt_div[lbm::kRegisterVariants] = {1, 1, 1, 2, 2, 2, 4, 4};
+    static const int blocks[lbm::kRegisterVariants] = {256, 256, 128, 256, 256, 128, 256, 256};
+    if (variant >= lbm::kRegisterVariants) {
+        const lbm::TmaConfig c = lbm::kTmaMenu[variant - lbm::kRegisterVariants];
+        block = 32 * (1 + c.consumer_warps);
+        cpt = (c.rows * nx + 32 * c.consumer_warps - 1) / (32 * c.consumer_warps);
+        return;
+    }
     const int V = 16 / (storage == LBM_STORAGE_F64 ? 8 : storage == LBM_STORAGE_F32 ? 4 : 2);
-    cpt = V / cpt_div[variant];
+    cpt = V / cpt_div[variant] > 0 ? V / cpt_div[variant] : 1;
     block = blocks[variant];
 }
 
@@ -98,7 +106,7 @@ struct lbm_solver {
     void* macros = nullptr;         // 4 * cells values (rho, jx, jy, jz)
     bool macros_fresh = false;
     double* scratch = nullptr;      // reduction partials (4 per block) + result (4)
-    unsigned long long* counts = nullptr;  // cavity-flag check counters
+    unsigned long long* counts = nullptr;  // cavity-flag check counters [0..1], kernel error flag [2]
     double* host_out = nullptr;     // pinned, 4 doubles
     float* staging = nullptr;       // 16-bit storage: one packed slot cuboid
     size_t staging_elems = 0;
@@ -112,6 +120,20 @@ struct lbm_solver {
 };
 
 namespace {
+
+int* err_flag(lbm_solver* s) { return reinterpret_cast<int*>(s->counts + 2); }
+
+// Reads and clears the kernels' timeout flag after the device is idle.
+int check_kernel_flag(lbm_solver* s)
+{
+    int flag = 0;
+    CK(cudaMemcpy(&flag, err_flag(s), sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy error flag");
+    if (flag) {
+        CK(cudaMemset(err_flag(s), 0, sizeof(int)), "cudaMemset error flag");
+        return fail(LBM_ERR_TIMEOUT, "a step kernel gave up waiting for its bulk copies (flag %d)", flag);
+    }
+    return LBM_OK;
+}
 
 int check_solver(const lbm_solver* s)
 {
@@ -172,7 +194,7 @@ int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, 
     int3 o, n;
     cudaError_t e;
     if (!origin && s->lid_y >= 0) {
-        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, s->p, s->lid_y, st);
+        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
     } else {
         if (origin) {
             int r = resolve_cuboid(s, origin, size, o, n);
@@ -201,6 +223,7 @@ int ensure_macros(lbm_solver* s)
     }
     if (!s->macros_fresh) {
         CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        if (int r = check_kernel_flag(s)) return r;
         CK(lbm::launch_macros(s->storage, s->dd, s->flags, s->g, s->last_alpha, s->p.lid_u, s->macros, 0),
            "compute_macros launch");
         CK(cudaDeviceSynchronize(), "compute_macros");
@@ -426,8 +449,10 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
     if ((e = cudaMalloc(&s->dd, dd_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc populations"));
     if ((e = cudaMalloc(&s->flags, flag_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc flags"));
     if ((e = cudaMalloc(&s->scratch, scratch_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc scratch"));
-    if ((e = cudaMalloc(&s->counts, 2 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMalloc(&s->counts, 4 * sizeof(unsigned long long))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMalloc counters"));
+    if ((e = cudaMemset(s->counts, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaMemset counters"));
     if ((e = cudaMallocHost(&s->host_out, 4 * sizeof(double))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMallocHost"));
     if ((e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
@@ -438,6 +463,9 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
     for (int f = 0; f < 6; ++f) bc.f[f] = prm->boundary[f];
     if ((e = lbm::launch_init(s->storage, s->dd, s->flags, s->g, bc, 0)) != cudaSuccess)
         return bail(cuda_fail(e, "init launch"));
+    if (!lbm::fast_variant_fits(s->storage, s->variant, s->g))
+        return bail(fail(LBM_ERR_UNSUPPORTED, "fast_variant %d needs more shared memory than this domain allows",
+                         s->variant));
     int r = refresh_path(s);
     if (r) return bail(r);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return bail(cuda_fail(e, "init"));
@@ -477,7 +505,7 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     info->last_step_was_alpha = s->last_alpha ? 1 : 0;
     info->fast_path = s->lid_y >= 0 ? 1 : 0;
     info->fast_variant = s->variant;
-    variant_shape(s->storage, s->variant, info->cells_per_thread, info->block_threads);
+    variant_shape(s->storage, s->variant, s->g.nx, info->cells_per_thread, info->block_threads);
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
@@ -553,11 +581,11 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             CK(cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             cudaError_t e = cudaSuccess;
             for (int i = 0; i < kGraphPairs && e == cudaSuccess; ++i) {
-                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, s->p, s->lid_y,
+                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, s->p, s->lid_y, err_flag(s),
                                           s->capture_stream);
                 if (e == cudaSuccess)
                     e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y,
-                                              s->capture_stream);
+                                              err_flag(s), s->capture_stream);
             }
             cudaError_t e2 = cudaStreamEndCapture(s->capture_stream, &graph);
             // captured launches are counted when the graph runs
@@ -592,7 +620,7 @@ int lbm_synchronize(lbm_solver* s)
     if (int r = check_solver(s)) return r;
     CK(cudaSetDevice(s->device), "cudaSetDevice");
     CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-    return LBM_OK;
+    return check_kernel_flag(s);
 }
 
 int lbm_fast_variant_count(void) { return lbm::kFastVariantCount; }
@@ -602,6 +630,9 @@ int lbm_set_fast_variant(lbm_solver* s, int32_t variant)
     if (int r = check_solver(s)) return r;
     if (variant < 0 || variant >= lbm::kFastVariantCount)
         return fail(LBM_ERR_INVALID_ARGUMENT, "variant %d not in [0, %d)", variant, lbm::kFastVariantCount);
+    CK(cudaSetDevice(s->device), "cudaSetDevice");
+    if (!lbm::fast_variant_fits(s->storage, variant, s->g))
+        return fail(LBM_ERR_UNSUPPORTED, "variant %d needs more shared memory than this domain allows", variant);
     if (variant != s->variant) drop_graph(s);
     s->variant = variant;
     return LBM_OK;
@@ -624,8 +655,9 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     int best_v = s->variant;
     auto run_pairs = [&](int v, int n) -> cudaError_t {
         for (int i = 0; i < n; ++i) {
-            cudaError_t e = lbm::launch_fast_step(s->storage, v, true, s->dd, s->g, s->p, s->lid_y, st);
-            if (e == cudaSuccess) e = lbm::launch_fast_step(s->storage, v, false, s->dd, s->g, s->p, s->lid_y, st);
+            cudaError_t e = lbm::launch_fast_step(s->storage, v, true, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+            if (e == cudaSuccess)
+                e = lbm::launch_fast_step(s->storage, v, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -634,8 +666,13 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (s->last_alpha && e == cudaSuccess)  // the timing runs alpha-first pairs from an even parity
-        e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y, st);
+        e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+    bool any = false;
     for (int v = 0; v < lbm::kFastVariantCount && e == cudaSuccess; ++v) {
+        if (!lbm::fast_variant_fits(s->storage, v, s->g)) {
+            if (ms_per_pair) ms_per_pair[v] = -1.f;
+            continue;
+        }
         e = run_pairs(v, 1);  // warm-up
         if (e == cudaSuccess) e = cudaEventRecord(e0, st);
         if (e == cudaSuccess) e = run_pairs(v, pairs);
@@ -645,7 +682,8 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
         ms /= (float)pairs;
         if (ms_per_pair) ms_per_pair[v] = ms;
-        if (e == cudaSuccess && (v == 0 || ms < best_ms)) {
+        if (e == cudaSuccess && (!any || ms < best_ms)) {
+            any = true;
             best_ms = ms;
             best_v = v;
         }
@@ -801,6 +839,7 @@ int lbm_reduce(lbm_solver* s, double out[4], void* stream)
        "reduce launch");
     CK(cudaMemcpyAsync(s->host_out, result, 4 * sizeof(double), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
     CK(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (int r = check_kernel_flag(s)) return r;
     for (int q = 0; q < 4; ++q) out[q] = s->host_out[q];
     return LBM_OK;
 }
@@ -819,6 +858,7 @@ const char* lbm_status_string(int status)
     case LBM_ERR_BUDGET: return "over memory budget";
     case LBM_ERR_NOT_READY: return "not ready";
     case LBM_ERR_NO_DEVICE: return "no CUDA device";
+    case LBM_ERR_TIMEOUT: return "device wait timed out";
     default: return "unknown status";
     }
 }

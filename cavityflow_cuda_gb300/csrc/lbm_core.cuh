@@ -261,6 +261,66 @@ __device__ __forceinline__ void collide_fluid_gravity(T* f, T inv_tau, T gx, T g
     alpha_gravity(f, rho, gx, gy, gz);
 }
 
+// ---------------------------------------------------------------------------
+// Collision of the shifted 16-bit storage modes.  Not bound to the
+// reference's operation order (those modes have no reference counterpart), so
+// it is written for throughput: moments from pair sums and differences, and
+// every multiply-add fused.  Same BGK model: for a direction pair with
+// projection u = c.j and weight w,
+//   feq+- - w = w (P + 4.5 u^2) +- 3 w u,   P = drho - 1.5 |j|^2,
+// relaxed as s += omega (feq - w - s).  oracle/lbm_oracle.c restates it with
+// fmaf, so the GPU result is checked bit for bit.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void relax_pair_shifted(float& sp, float& sm, float w3, float w45, float wP, float u,
+                                                   float omega)
+{
+    const float even = __fmaf_rn(w45, u * u, wP);
+    const float odd = w3 * u;
+    sp = __fmaf_rn(omega, (even + odd) - sp, sp);
+    sm = __fmaf_rn(omega, (even - odd) - sm, sm);
+}
+
+__device__ __forceinline__ void collide_shifted(float* s, float omega)
+{
+    const float a01 = s[0] + s[1], d01 = s[0] - s[1];
+    const float a23 = s[2] + s[3], d23 = s[2] - s[3];
+    const float a45 = s[4] + s[5], d45 = s[4] - s[5];
+    const float a67 = s[6] + s[7], d67 = s[6] - s[7];
+    const float a89 = s[8] + s[9], d89 = s[8] - s[9];
+    const float a1011 = s[10] + s[11], d1011 = s[10] - s[11];
+    const float a1213 = s[12] + s[13], d1213 = s[12] - s[13];
+    const float a1415 = s[14] + s[15], d1415 = s[14] - s[15];
+    const float a1617 = s[16] + s[17], d1617 = s[16] - s[17];
+    const float drho = ((a01 + a23) + (a45 + a67)) + ((a89 + a1011) + (a1213 + a1415)) + (a1617 + s[18]);
+    const float jx = ((d01 + d45) + (d67 + d89)) + d1011;
+    const float jy = ((d23 + d45) - d67) + (d1213 + d1415);
+    const float jz = ((d89 - d1011) + (d1213 - d1415)) + d1617;
+    const float vel2 = __fmaf_rn(jz, jz, __fmaf_rn(jy, jy, jx * jx));
+    const float P = __fmaf_rn(-1.5f, vel2, drho);
+    const float wa = 1.0f / 18.0f, wd = 1.0f / 36.0f;
+    const float waP = wa * P, wdP = wd * P;
+    const float wa3 = 3.0f * wa, wa45 = 4.5f * wa, wd3 = 3.0f * wd, wd45 = 4.5f * wd;
+    relax_pair_shifted(s[0], s[1], wa3, wa45, waP, jx, omega);
+    relax_pair_shifted(s[2], s[3], wa3, wa45, waP, jy, omega);
+    relax_pair_shifted(s[4], s[5], wd3, wd45, wdP, jx + jy, omega);
+    relax_pair_shifted(s[6], s[7], wd3, wd45, wdP, jx - jy, omega);
+    relax_pair_shifted(s[8], s[9], wd3, wd45, wdP, jx + jz, omega);
+    relax_pair_shifted(s[10], s[11], wd3, wd45, wdP, jx - jz, omega);
+    relax_pair_shifted(s[12], s[13], wd3, wd45, wdP, jy + jz, omega);
+    relax_pair_shifted(s[14], s[15], wd3, wd45, wdP, jy - jz, omega);
+    relax_pair_shifted(s[16], s[17], wa3, wa45, waP, jz, omega);
+    s[18] = __fmaf_rn(omega, (1.0f / 3.0f) * P - s[18], s[18]);
+}
+
+// Collision dispatch by storage: the reference's arithmetic for F64/F32, the
+// fused form above for the shifted 16-bit modes.
+template <class St>
+__device__ __forceinline__ void collide(typename St::T* f, typename St::T inv_tau)
+{
+    if constexpr (St::shifted) collide_shifted(f, inv_tau);
+    else collide_fluid(f, inv_tau);
+}
+
 // VELOCITY_INJECTION: feq(rho = 1, j = (U, 0, 0)) (lbm_alpha.cu:376-511,
 // lbm_beta.cu:661-732); rho0 = 0 gives the deviation form for shifted storage.
 template <typename T>

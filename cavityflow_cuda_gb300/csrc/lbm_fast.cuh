@@ -67,17 +67,49 @@ struct Vio {
         for (int v = 0; v < N; ++v) x.b[v] = St::store(a[v]);
         *reinterpret_cast<raw*>(p) = x.u;
     }
+    // Storage-typed access: 16-bit populations stay packed in registers and
+    // are converted one cell at a time, which halves their register footprint.
+    __device__ static void load_raw(const bits* p, bits (&a)[N])
+    {
+        Pack x;
+        x.u = *reinterpret_cast<const raw*>(p);
+#pragma unroll
+        for (int v = 0; v < N; ++v) a[v] = x.b[v];
+    }
+    __device__ static void store_raw(bits* p, const bits (&a)[N])
+    {
+        Pack x;
+#pragma unroll
+        for (int v = 0; v < N; ++v) x.b[v] = a[v];
+        *reinterpret_cast<raw*>(p) = x.u;
+    }
 };
 
-template <class St, int CPT, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
-                                                          const typename St::T inv_tau,
-                                                          const typename St::T lid_u, const int lid_y)
+// Warp shuffles of storage elements (16-bit patterns travel in 32-bit lanes).
+template <typename B>
+__device__ __forceinline__ B shfl_up_bits(B v, int d)
+{
+    if constexpr (sizeof(B) == 2) return (B)__shfl_up_sync(0xffffffffu, (unsigned)v, d);
+    else return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <typename B>
+__device__ __forceinline__ B shfl_down_bits(B v, int d)
+{
+    if constexpr (sizeof(B) == 2) return (B)__shfl_down_sync(0xffffffffu, (unsigned)v, d);
+    else return __shfl_down_sync(0xffffffffu, v, d);
+}
+
+// Alpha step of the CPT cells owned by thread index t of one domain (t runs
+// over groups x rows x planes: t = ((z-1) * ny + (y-1)) * G + group).
+template <class St, int CPT>
+__device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, const Grid& g,
+                                            const typename St::T inv_tau, const typename St::T lid_u,
+                                            const int lid_y, const long long t)
 {
     using T = typename St::T;
+    using bits = typename St::bits;
     using IO = Vio<St, CPT>;
     const int G = (g.nx + CPT - 1) / CPT;
-    const long long t = (long long)blockIdx.x * BLOCK + threadIdx.x;
     const long long total = (long long)G * g.ny * g.nz;
     if (t >= total) return;
     const int gi = (int)(t % G);
@@ -87,9 +119,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
     const int x0 = 1 + gi * CPT;
     const long long base = g.idx(x0, y, z);
 
-    T f[Q][CPT];
+    bits f[Q][CPT];
 #pragma unroll
-    for (int k = 0; k < Q; ++k) IO::load(dd + k * g.S + base, f[k]);
+    for (int k = 0; k < Q; ++k) IO::load_raw(dd + k * g.S + base, f[k]);
 
     const bool lid = (y == lid_y);
     const T rho0 = St::shifted ? T(0) : T(1);
@@ -98,25 +130,36 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
         if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
         T c[Q];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) c[k] = f[k][v];
+        for (int k = 0; k < Q; ++k) c[k] = St::load(f[k][v]);
         if (lid) inject(c, rho0, lid_u);
-        else collide_fluid(c, inv_tau);
+        else collide<St>(c, inv_tau);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) f[opp(k)][v] = c[k];  // population k -> slot opp(k)
+        for (int k = 0; k < Q; ++k) f[opp(k)][v] = St::store(c[k]);  // population k -> slot opp(k)
     }
 #pragma unroll
-    for (int k = 0; k < Q; ++k) IO::store(dd + k * g.S + base, f[k]);
+    for (int k = 0; k < Q; ++k) IO::store_raw(dd + k * g.S + base, f[k]);
 }
 
 template <class St, int CPT, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
-                                                         const typename St::T inv_tau,
-                                                         const typename St::T lid_u, const int lid_y)
+__global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                          const typename St::T inv_tau,
+                                                          const typename St::T lid_u, const int lid_y)
+{
+    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
+}
+
+// Beta step of the CPT cells owned by thread index t of one domain.  All 32
+// lanes of the warp must call it together, with consecutive t (they exchange
+// edge elements by shuffles); lanes past the domain's end take part in the
+// shuffles only.
+template <class St, int CPT>
+__device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, const Grid& g,
+                                           const typename St::T inv_tau, const typename St::T lid_u,
+                                           const int lid_y, const long long t)
 {
     using T = typename St::T;
     using IO = Vio<St, CPT>;
     const int G = (g.nx + CPT - 1) / CPT;
-    const long long t = (long long)blockIdx.x * BLOCK + threadIdx.x;
     const long long total = (long long)G * g.ny * g.nz;
     const bool active = t < total;
     const int lane = threadIdx.x & 31;
@@ -129,38 +172,39 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __re
     // The neighbouring group of the same row is held by the adjacent lane.
     const bool left_in = gi > 0 && lane > 0;
     const bool right_in = gi < G - 1 && lane < 31;
-    const unsigned full = 0xffffffffu;
 
     // p[k][v]: value of slot k at (cell x0+v) + c_k, i.e. population opp(k)
-    // arriving at cell x0+v.  edge[k]: the aligned element of slot k that lies
-    // outside this thread's shifted window (kept to rewrite it unchanged).
-    T p[Q][CPT];
-    T edge[Q];
+    // arriving at cell x0+v, kept in storage type.  edge[k]: the aligned
+    // element of slot k that lies outside this thread's shifted window (kept to
+    // rewrite it unchanged).
+    using bits = typename St::bits;
+    bits p[Q][CPT];
+    bits edge[Q];
 
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
         const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
-        T a[CPT];
-        if (active) IO::load(dd + rb, a);
+        bits a[CPT];
+        if (active) IO::load_raw(dd + rb, a);
         else {
 #pragma unroll
-            for (int v = 0; v < CPT; ++v) a[v] = T(0);
+            for (int v = 0; v < CPT; ++v) a[v] = bits(0);
         }
         if constexpr (cx == 0) {
 #pragma unroll
             for (int v = 0; v < CPT; ++v) p[k][v] = a[v];
-            edge[k] = T(0);
+            edge[k] = bits(0);
         } else if constexpr (cx == 1) {
-            T nb = __shfl_down_sync(full, a[0], 1);
-            if (active && !right_in) nb = St::load(dd[rb + CPT]);
+            bits nb = shfl_down_bits(a[0], 1);
+            if (active && !right_in) nb = dd[rb + CPT];
 #pragma unroll
             for (int v = 0; v < CPT - 1; ++v) p[k][v] = a[v + 1];
             p[k][CPT - 1] = nb;
             edge[k] = a[0];
         } else {
-            T pb = __shfl_up_sync(full, a[CPT - 1], 1);
-            if (active && !left_in) pb = St::load(dd[rb - 1]);
+            bits pb = shfl_up_bits(a[CPT - 1], 1);
+            if (active && !left_in) pb = dd[rb - 1];
             p[k][0] = pb;
 #pragma unroll
             for (int v = 1; v < CPT; ++v) p[k][v] = a[v - 1];
@@ -175,11 +219,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __re
         if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
         T c[Q];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) c[opp(k)] = p[k][v];
+        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load(p[k][v]);
         if (lid) inject(c, rho0, lid_u);
-        else collide_fluid(c, inv_tau);
+        else collide<St>(c, inv_tau);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) p[k][v] = c[k];  // population k -> slot k at x + c_k
+        for (int k = 0; k < Q; ++k) p[k][v] = St::store(c[k]);  // population k -> slot k at x + c_k
     }
 
     static_for<0, Q>([&](auto kc) {
@@ -187,41 +231,49 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __re
         constexpr int cx = dir_x(k);
         const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
         if constexpr (cx == 0) {
-            if (active) IO::store(dd + rb, p[k]);
+            if (active) IO::store_raw(dd + rb, p[k]);
         } else if constexpr (cx == 1) {
             // aligned element 0 belongs to cell x0-1 (left lane's last cell)
-            const T from_left = __shfl_up_sync(full, p[k][CPT - 1], 1);
+            const bits from_left = shfl_up_bits(p[k][CPT - 1], 1);
             if (active) {
-                T o[CPT];
+                bits o[CPT];
 #pragma unroll
                 for (int v = 1; v < CPT; ++v) o[v] = p[k][v - 1];
                 if (left_in || gi == 0) {
                     o[0] = left_in ? from_left : edge[k];
-                    IO::store(dd + rb, o);
+                    IO::store_raw(dd + rb, o);
                 } else {
 #pragma unroll
-                    for (int v = 1; v < CPT; ++v) dd[rb + v] = St::store(o[v]);
+                    for (int v = 1; v < CPT; ++v) dd[rb + v] = o[v];
                 }
-                if (!right_in && x0 + CPT - 1 <= g.nx) dd[rb + CPT] = St::store(p[k][CPT - 1]);
+                if (!right_in && x0 + CPT - 1 <= g.nx) dd[rb + CPT] = p[k][CPT - 1];
             }
         } else {
             // aligned element CPT-1 belongs to cell x0+CPT (right lane's first cell)
-            const T from_right = __shfl_down_sync(full, p[k][0], 1);
+            const bits from_right = shfl_down_bits(p[k][0], 1);
             if (active) {
-                T o[CPT];
+                bits o[CPT];
 #pragma unroll
                 for (int v = 0; v < CPT - 1; ++v) o[v] = p[k][v + 1];
                 if (right_in || gi == G - 1) {
                     o[CPT - 1] = right_in ? from_right : edge[k];
-                    IO::store(dd + rb, o);
+                    IO::store_raw(dd + rb, o);
                 } else {
 #pragma unroll
-                    for (int v = 0; v < CPT - 1; ++v) dd[rb + v] = St::store(o[v]);
+                    for (int v = 0; v < CPT - 1; ++v) dd[rb + v] = o[v];
                 }
-                if (!left_in) dd[rb - 1] = St::store(p[k][0]);
+                if (!left_in) dd[rb - 1] = p[k][0];
             }
         }
     });
+}
+
+template <class St, int CPT, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
+                                                         const typename St::T inv_tau,
+                                                         const typename St::T lid_u, const int lid_y)
+{
+    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
 }
 
 // Launch menu shared by every storage type: (cells per thread as a fraction
@@ -231,7 +283,7 @@ struct FastVariant {
     int block;
     int minb;
 };
-constexpr int kFastVariants = 6;
+constexpr int kFastVariants = 8;
 constexpr FastVariant kFastMenu[kFastVariants] = {
     {1, 256, 1},  // 16-byte vectors, registers unconstrained
     {1, 256, 2},  // 16-byte vectors, <= 128 registers
@@ -239,6 +291,8 @@ constexpr FastVariant kFastMenu[kFastVariants] = {
     {2, 256, 2},  // 8-byte vectors, <= 128 registers
     {2, 256, 3},  // 8-byte vectors, <= 85 registers
     {2, 128, 5},  // 8-byte vectors, <= 102 registers
+    {4, 256, 2},  // 4-byte vectors (FP64: one cell), <= 128 registers
+    {4, 256, 3},  // 4-byte vectors (FP64: one cell), <= 85 registers
 };
 
 template <class St, int VARIANT>
@@ -246,7 +300,8 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
 {
     using T = typename St::T;
     constexpr FastVariant fv = kFastMenu[VARIANT];
-    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div;
+    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div > 0
+                            ? (16 / (int)sizeof(typename St::bits)) / fv.cpt_div : 1;
     const int G = (g.nx + CPT - 1) / CPT;
     const long long threads = (long long)G * g.ny * g.nz;
     const int blocks = (int)((threads + fv.block - 1) / fv.block);
@@ -267,6 +322,8 @@ cudaError_t launch_fast_menu(int variant, bool alpha, void* dd, const Grid& g, c
     case 3: return launch_fast_variant<St, 3>(alpha, dd, g, p, lid_y, st);
     case 4: return launch_fast_variant<St, 4>(alpha, dd, g, p, lid_y, st);
     case 5: return launch_fast_variant<St, 5>(alpha, dd, g, p, lid_y, st);
+    case 6: return launch_fast_variant<St, 6>(alpha, dd, g, p, lid_y, st);
+    case 7: return launch_fast_variant<St, 7>(alpha, dd, g, p, lid_y, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -52,7 +52,7 @@ __global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t*
 #pragma unroll
         for (int k = 0; k < Q; ++k) f[k] = St::load(dd[k * g.S + c0]);
         if (kGravity) collide_fluid_gravity(f, inv_tau, T(prm.gx), T(prm.gy), T(prm.gz));
-        else collide_fluid(f, inv_tau);
+        else collide<St>(f, inv_tau);
     } else {
         inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
         if (kGravity) alpha_gravity(f, T(1), T(prm.gx), T(prm.gy), T(prm.gz));
@@ -83,7 +83,7 @@ __global__ void beta_general(typename St::bits* __restrict__ dd, const uint8_t* 
     T f[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) f[opp(k)] = St::load(dd[pos[k]]);
-    if (fl == kFluid) collide_fluid(f, T(prm.inv_tau));
+    if (fl == kFluid) collide<St>(f, T(prm.inv_tau));
     else if (fl == kInjection) inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
     // GHOST_LAYER (and any other value): streamed through unchanged
 #pragma unroll
@@ -370,9 +370,36 @@ cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned lo
     return cudaGetLastError();
 }
 
-cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
-                             int lid_y, cudaStream_t st)
+bool fast_variant_fits(int storage, int variant, const Grid& g)
 {
+    if (variant < 0 || variant >= kFastVariantCount) return false;
+    if (variant < kRegisterVariants) return true;
+    const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
+    const int elem = storage == 0 ? 8 : storage == 1 ? 4 : 2;
+    int dev = 0, max_optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    if (cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
+    const size_t stage = (size_t)Q * c.rows * g.P * elem;
+    // 1 KiB left for the kernel's static shared memory
+    return (size_t)c.stages * stage + 2 * (size_t)c.stages * sizeof(uint64_t) + 16 + 1024 <= (size_t)max_optin;
+}
+
+cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
+                             int lid_y, int* err, cudaStream_t st)
+{
+    if (variant >= kRegisterVariants && variant < kFastVariantCount) {
+        const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
+        cudaError_t e;
+        switch (storage) {
+        case 0: e = launch_tma_f64(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 1: e = launch_tma_f32(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 2: e = launch_tma_f16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 3: e = launch_tma_bf16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        default: return cudaErrorInvalidValue;
+        }
+        if (e == cudaSuccess) count_launch();
+        return e;
+    }
     count_launch();
     switch (storage) {
     case 0: return launch_fast_f64(variant, alpha, dd, g, p, lid_y, st);

@@ -26,11 +26,26 @@ void add_launches(long long n);
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
 cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
-// Vectorised box-cavity step; `variant` indexes the launch menu of
-// lbm_fast.cuh (cells per thread, block size, blocks per SM).
-constexpr int kFastVariantCount = 6;
+// Box-cavity step.  Variants 0..kRegisterVariants-1 index the register
+// kernels of lbm_fast.cuh (cells per thread, block size, blocks per SM); the
+// rest index kTmaMenu, the row-pipelined bulk-copy kernels of lbm_tma.cuh.
+// A variant that does not fit the domain returns cudaErrorInvalidValue
+// before launching anything.  `err` receives the bulk-copy kernels' timeout flag.
+constexpr int kRegisterVariants = 8;
+struct TmaConfig {
+    int rows;            // rows per work unit
+    int stages;          // shared-memory buffers
+    int consumer_warps;  // warps that collide (plus one producer warp)
+};
+constexpr int kTmaVariants = 6;
+constexpr TmaConfig kTmaMenu[kTmaVariants] = {
+    {1, 3, 6}, {1, 4, 6}, {2, 2, 8}, {2, 3, 8}, {1, 2, 4}, {4, 2, 8},
+};
+constexpr int kFastVariantCount = kRegisterVariants + kTmaVariants;
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
-                             int lid_y, cudaStream_t st);
+                             int lid_y, int* err, cudaStream_t st);
+// Whether a variant fits this domain (shared memory of the bulk-copy kernels).
+bool fast_variant_fits(int storage, int variant, const Grid& g);
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
@@ -39,6 +54,14 @@ cudaError_t launch_fast_f16s(int variant, bool alpha, void* dd, const Grid& g, c
                              cudaStream_t st);
 cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                               cudaStream_t st);
+cudaError_t launch_tma_f64(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                           int consumer_warps, int* err, cudaStream_t st);
+cudaError_t launch_tma_f32(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                           int consumer_warps, int* err, cudaStream_t st);
+cudaError_t launch_tma_f16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                            int consumer_warps, int* err, cudaStream_t st);
+cudaError_t launch_tma_bf16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows,
+                             int stages, int consumer_warps, int* err, cudaStream_t st);
 cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,
                                 const Params& p, int3 origin, int3 size, cudaStream_t st);
 cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,

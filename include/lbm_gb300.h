@@ -52,7 +52,8 @@ typedef enum lbm_status {
     LBM_ERR_IO = 7,               /* file could not be read or written             */
     LBM_ERR_BUDGET = 8,           /* request does not fit the memory budget        */
     LBM_ERR_NOT_READY = 9,        /* result requested before it exists             */
-    LBM_ERR_NO_DEVICE = 10        /* no CUDA device visible                        */
+    LBM_ERR_NO_DEVICE = 10,       /* no CUDA device visible                        */
+    LBM_ERR_TIMEOUT = 11          /* a kernel gave up a bounded device-side wait   */
 } lbm_status;
 
 /* Flag values, src/common.h:54-61. */
@@ -202,13 +203,16 @@ int lbm_synchronize(lbm_solver* solver);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the vectorised kernels (cells per thread,
- * threads per block, blocks per SM). */
+/* Number of launch variants of the box-cavity kernels: register-blocked
+ * vector kernels (cells per thread, threads per block, blocks per SM) and
+ * row-pipelined bulk-copy kernels (rows per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
-/* Selects a variant for subsequent steps. */
+/* Selects a variant for subsequent steps; LBM_ERR_UNSUPPORTED if it needs more
+ * shared memory than this domain allows. */
 int lbm_set_fast_variant(lbm_solver* solver, int32_t variant);
-/* Times every variant on this solver's domain (`pairs` alpha/beta pairs each,
- * CUDA events) and selects the fastest.  The populations are saved to a
+/* Times every variant that fits this solver's domain (`pairs` alpha/beta pairs
+ * each, CUDA events; -1 for a variant that does not fit) and selects the
+ * fastest.  The populations are saved to a
  * temporary device buffer first and restored afterwards, so the simulation
  * state and step counter are unchanged.  ms_per_pair (optional) receives one
  * time per variant.  Synchronous. */

@@ -129,6 +129,65 @@ class Oracle(_Lib):
         fn(_ptr(dd), _ptr(flags), nx, ny, nz, int(bool(last_was_alpha)), _ptr(out))
         return out  # mass, px, py, pz
 
+    # -- shifted 16-bit storage (the solver's FP16/BF16 extension) --------------
+    # kind 0: FP16, 1: BF16.  Arrays are uint16 bit patterns of f - w.
+    def init_s(self, nx, ny, nz, bc=(OBSTACLE,) * 6):
+        dd = np.zeros((19, nz + 2, ny + 2, nx + 2), dtype=np.uint16)
+        flags = np.zeros((nz + 2, ny + 2, nx + 2), dtype=np.int32)
+        fn = self.lib.orc_init_s
+        fn.argtypes = [_P, _P, _I, _I, _I, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, (C.c_int32 * 6)(*bc))
+        return dd, flags
+
+    def step_s(self, dd, flags, counter, inv_tau, lid_u, kind, origin=None, size=None):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        origin = (0, 0, 0) if origin is None else origin
+        size = (nx + 2, ny + 2, nz + 2) if size is None else size
+        fn = self.lib.orc_beta_s if counter & 1 else self.lib.orc_alpha_s
+        fn.argtypes = [_P, _P, _I, _I, _I, C.c_float, C.c_float, _I, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, int(kind), _i3(origin), _i3(size))
+
+    def run_cavity_s(self, nx, ny, nz, kind, inv_tau, lid_u, steps, lid=True):
+        dd, flags = self.init_s(nx, ny, nz)
+        if lid:
+            self.set_lid(flags)
+        for i in range(steps):
+            self.step_s(dd, flags, i, inv_tau, lid_u, kind)
+        return dd, flags
+
+    def unshift(self, dd, kind):
+        """float32 populations f = s + w of a shifted 16-bit array."""
+        if kind == 0:
+            f = dd.view(np.float16).astype(np.float32)
+        else:
+            f = (dd.astype(np.uint32) << 16).view(np.float32)
+        w = np.array([np.float32(1) / np.float32(18)] * 4 + [np.float32(1) / np.float32(36)] * 12 +
+                     [np.float32(1) / np.float32(18)] * 2 + [np.float32(1) / np.float32(3)], dtype=np.float32)
+        return f + w[:, None, None, None]
+
+    def macros_s(self, dd, flags, last_was_alpha, lid_u, kind):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        out = [np.zeros(flags.shape, dtype=np.float32) for _ in range(4)]
+        fn = self.lib.orc_macros_s
+        fn.argtypes = [_P, _P, _I, _I, _I, _I, C.c_float, _I, _P, _P, _P, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, int(bool(last_was_alpha)), lid_u, int(kind), *[_ptr(o) for o in out])
+        return out
+
+    def reduce_s(self, dd, flags, last_was_alpha, kind):
+        nz, ny, nx = (s - 2 for s in flags.shape)
+        out = np.zeros(4, dtype=np.float64)
+        fn = self.lib.orc_reduce_s
+        fn.argtypes = [_P, _P, _I, _I, _I, _I, _I, _P]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, int(bool(last_was_alpha)), int(kind), _ptr(out))
+        return out
+
+    def to_half(self, x: np.ndarray, kind: int) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        fn = self.lib.orc_float_to_bf16 if kind else self.lib.orc_float_to_half
+        fn.argtypes = [C.c_float]
+        fn.restype = C.c_uint16
+        return np.array([fn(float(v)) for v in x.ravel()], dtype=np.uint16).reshape(x.shape)
+
     # -- convenience: the reference's time loop (src/CController.cpp:1278-1287) --
     def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):
         if counter & 1:

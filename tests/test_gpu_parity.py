@@ -91,18 +91,29 @@ def test_odd_shapes_match_oracle(gpu, oracle, dtype, n, steps):
         assert same_bits(s.get_all(), want)
 
 
-@pytest.mark.parametrize("variant", range(6))
+@pytest.mark.parametrize("variant", range(14))
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_every_launch_variant_matches_oracle(gpu, oracle, variant, dtype):
-    """Each cells-per-thread / block-size variant of the vectorised kernels."""
+    """Each launch variant: register-blocked vector kernels (0-7) and the
+    row-pipelined bulk-copy kernels (8-13)."""
     _, itau = orc.tau_of(0.032, dtype)
     lid = dtype(0.07)
+    from cavityflow_cuda_gb300 import LbmError
+
+    ran = 0
     for n, steps in (((37, 9, 5), 13), ((300, 4, 3), 6), ((5, 6, 7), 9)):
         want, _ = oracle.run_cavity(*n, dtype, itau, lid, steps)
-        with solver(n, dtype, itau, lid, fast_variant=variant) as s:
+        try:
+            s = solver(n, dtype, itau, lid, fast_variant=variant)
+        except LbmError as e:  # a bulk-copy variant whose buffers exceed shared memory
+            assert e.status == 5
+            continue
+        with s:
             assert s.info()["fast_variant"] == variant
             s.run(steps)
             assert same_bits(s.get_all(), want), (variant, n)
+            ran += 1
+    assert ran >= 2
 
 
 def test_autotune_keeps_state(gpu):

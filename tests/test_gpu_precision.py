@@ -1,0 +1,100 @@
+"""FP16 / BF16 shifted-population storage (f - w stored in 16 bits, collision
+in FP32 registers): bit-identical to the oracle's restatement of the same
+arithmetic, for every launch variant, plus the macroscopic getters and the
+FP64 reduction; and its velocity error against an FP64 run of this solver."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+KIND = {"f16s": 0, "bf16s": 1}
+
+
+def shifted_solver(n, storage, inv_tau, lid, **kw):
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    return CLbmSolverGB300(n, inv_tau, lid, storage=storage, **kw)
+
+
+@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+@pytest.mark.parametrize("variant", range(14))
+def test_shifted_storage_matches_oracle(gpu, oracle, storage, variant):
+    _, itau = orc.tau_of(0.0192, np.float32)
+    lid = np.float32(0.08)
+    from cavityflow_cuda_gb300 import LbmError
+
+    ran = 0
+    for n, steps in (((45, 9, 5), 13), ((300, 4, 3), 8), ((6, 7, 8), 11)):
+        dd, _ = oracle.run_cavity_s(*n, KIND[storage], itau, lid, steps)
+        want = oracle.unshift(dd, KIND[storage])
+        try:
+            s = shifted_solver(n, storage, itau, lid, fast_variant=variant)
+        except LbmError as e:  # a bulk-copy variant whose buffers exceed shared memory
+            assert e.status == 5
+            continue
+        with s:
+            s.run(steps)
+            got = s.get_all()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (storage, variant, n)
+        ran += 1
+    assert ran >= 2
+
+
+@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+def test_shifted_macros_and_reduce_match_oracle(gpu, oracle, storage):
+    _, itau = orc.tau_of(0.032, np.float32)
+    lid = np.float32(0.06)
+    n = (14, 10, 9)
+    for steps in (9, 10):
+        dd, flags = oracle.run_cavity_s(*n, KIND[storage], itau, lid, steps)
+        rho, jx, jy, jz = oracle.macros_s(dd, flags, bool(steps & 1), lid, KIND[storage])
+        want_red = oracle.reduce_s(dd, flags, bool(steps & 1), KIND[storage])
+        with shifted_solver(n, storage, itau, lid) as s:
+            s.run(steps)
+            full = ((0, 0, 0), (n[0] + 2, n[1] + 2, n[2] + 2))
+            u = s.getVelocities(*full)
+            r = s.getDensities(*full)
+            red = s.reduce()
+        assert np.array_equal(r, rho) and np.array_equal(u[0], jx) and np.array_equal(u[1], jy)
+        assert np.array_equal(u[2], jz)
+        assert np.allclose(red, want_red, rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+def test_shifted_population_roundtrip(gpu, storage):
+    """set -> get of populations converts f <-> f - w exactly where 16 bits hold it."""
+    rng = np.random.default_rng(5)
+    n = (10, 9, 8)
+    with shifted_solver(n, storage, 1.7, 0.05) as s:
+        base = s.get_all()
+        w = base[:, 0, 0, 0]
+        src = (w[:, None, None, None] + 0.001 * rng.standard_normal((19, 3, 4, 5))).astype(np.float32)
+        s.setDensityDistributions(src, (2, 2, 2), (5, 4, 3))
+        got = s.getDensityDistributions((2, 2, 2), (5, 4, 3))
+        tol = 1e-6 if storage == "f16s" else 1e-5
+        assert np.abs(got - src).max() < tol
+
+
+def test_fp16_velocity_error_against_fp64(gpu):
+    """L2 velocity error of FP16/BF16 storage against an FP64 run of this
+    solver on a 48^3 cavity after 1000 steps (the full-size measurement is
+    bench.py's precision report)."""
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    n, steps = (48, 48, 48), 1000
+    _, itau64 = orc.tau_of(0.0512, np.float64)
+    with CLbmSolverGB300(n, itau64, 0.1, storage="f64") as s:
+        s.run(steps)
+        u64 = s.getVelocities().astype(np.float64)
+    errs = {}
+    for storage in ("f32", "f16s", "bf16s"):
+        _, itau = orc.tau_of(0.0512, np.float32)
+        with CLbmSolverGB300(n, itau, np.float32(0.1), storage=storage) as s:
+            s.run(steps)
+            u = s.getVelocities().astype(np.float64)
+        errs[storage] = np.sqrt(((u - u64) ** 2).sum() / (u64 ** 2).sum())
+    assert errs["f32"] < 1e-4, errs   # unshifted FP32 loses digits in f - w itself
+    assert errs["f16s"] < 1e-3, errs
+    print("L2 velocity error vs FP64:", errs)

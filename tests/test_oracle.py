@@ -125,3 +125,31 @@ def test_macros_of_lid_and_walls(oracle):
     assert (rho[0] == 0).all() and (jx[:, 0] == 0).all()
     # interior fluid: sums of post-collision populations
     assert np.all(np.abs(rho[1:-1, 1:-2, 1:-1] - 1.0) < 0.05)
+
+
+def test_16bit_conversions_round_to_nearest_even(oracle):
+    """The oracle's FP16/BF16 conversions are IEEE round-to-nearest-even
+    (checked against numpy's float16 and torch's bfloat16)."""
+    import torch
+
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.standard_normal(3000).astype(np.float32) * s for s in (1e-7, 1e-5, 1e-2, 1, 3e4)] +
+                       [np.array([0, -0.0, 65504, 65519.99, 5.96e-8, 2.98e-8, 2.99e-8, np.inf], np.float32)])
+    with np.errstate(over="ignore"):
+        assert np.array_equal(oracle.to_half(x, 0), x.astype(np.float16).view(np.uint16))
+    assert np.array_equal(oracle.to_half(x, 1),
+                          torch.from_numpy(x).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16))
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_shifted_storage_tracks_fp32(oracle, kind):
+    """FP16/BF16 deviation storage follows the FP32 run closely on a small cavity."""
+    _, itau = orc.tau_of(0.032, np.float32)
+    n, steps = (12, 10, 8), 60
+    ref, flags = oracle.run_cavity(*n, np.float32, itau, np.float32(0.05), steps)
+    dd, _ = oracle.run_cavity_s(*n, kind, itau, np.float32(0.05), steps)
+    assert (dd[:, 0, 0, 0] == 0).all()
+    _, ux, uy, uz = oracle.macros(ref, flags, False, np.float32(0.05))
+    _, sx, sy, sz = oracle.macros_s(dd, flags, False, np.float32(0.05), kind)
+    err = np.sqrt(((sx - ux) ** 2 + (sy - uy) ** 2 + (sz - uz) ** 2).sum() / (ux ** 2 + uy ** 2 + uz ** 2).sum())
+    assert err < (2e-3 if kind == 0 else 2e-2), err
