@@ -56,6 +56,13 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch", "precision"],
+                    help="cavity: the single-domain benchmark line; batch / precision: the extension measurements")
+    ap.add_argument("--no-extensions", action="store_true", help="skip the bounded extension measurements")
+    ap.add_argument("--batch-count", type=int, default=512)
+    ap.add_argument("--batch-steps", type=int, default=2000)
+    ap.add_argument("--precision-size", type=int, default=512)
+    ap.add_argument("--precision-steps", type=int, default=5000)
     return ap.parse_args()
 
 
@@ -251,10 +258,132 @@ def profile_traffic(a, kernel):
     return e["dram_bytes_per_launch"] * (a.size ** 3) / float(e["cells"])
 
 
+def batch_measure(storage, count, steps, device=0, autotune=True):
+    """Aggregate MLUPS of the seeded batch of box cavities (512 edges in
+    [16,96], lid in [0.02,0.1], Re log-uniform in [10,2000], seed 0), all
+    advanced together; CUDA events around `steps` steps on one stream."""
+    import torch
+
+    from cavityflow_cuda_gb300 import LbmBatch
+    from cavityflow_cuda_gb300.workloads import batch_workload
+
+    cav = batch_workload(count=count, seed=0)
+    stream = torch.cuda.Stream()
+    with LbmBatch([c.solver_args(storage) for c in cav], storage=storage, device=device) as b:
+        tuned = b.autotune(pairs=3) if autotune else (b.info()["fast_variant"], [])
+        b.run(4, stream=stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(steps, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        info = b.info()
+    lups = float(info["interior_cells"]) * steps
+    return {"storage": storage, "domains": count, "steps": steps, "interior_cells": info["interior_cells"],
+            "mlups": round(lups / (ms / 1e3) / 1e6, 1), "ms": round(ms, 2), "variant": tuned[0],
+            "variant_ms_per_pair": [round(v, 4) for v in tuned[1]],
+            "device_gb": round(info["device_bytes"] / 1e9, 3)}
+
+
+def single_measure(storage, n, steps, device=0):
+    """MLUPS of one n^3 cavity (the comparison point of the batch)."""
+    import torch
+
+    from cavityflow_cuda_gb300 import CLbmSolverGB300, derive_lattice
+
+    lat = derive_lattice(velocity=(0.05, 0, 0), viscosity=0.0192, domain_size=(n, n, n), storage=storage)
+    stream = torch.cuda.Stream()
+    with CLbmSolverGB300((n, n, n), lat["inv_tau"], lat["velocity"][0], storage=storage, device=device) as s:
+        s.run(4, stream=stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.run(steps, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+    return float(n) ** 3 * steps / (ms / 1e3) / 1e6
+
+
+def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
+    """L2 and max velocity error of FP32, FP16-shifted and BF16-shifted storage
+    against an FP64 run of this solver (same cavity), the FP64 mass drift, and
+    each storage's MLUPS (CUDA events around the run)."""
+    import torch
+
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+    from cavityflow_cuda_gb300.workloads import lattice_tau
+
+    res = {"domain": [n] * 3, "steps": steps, "lid": lid, "nu": nu, "re": round(n * lid / nu, 1)}
+    fields = {}
+    for storage in ("f64", "f32", "f16s", "bf16s"):
+        _, inv_tau = lattice_tau(nu, storage)
+        T = np.float64 if storage == "f64" else np.float32
+        stream = torch.cuda.Stream()
+        with CLbmSolverGB300((n, n, n), inv_tau, float(T(lid)), storage=storage, device=device) as s:
+            m0 = s.reduce()[0]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run(steps, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            fields[storage] = s.getVelocities().astype(np.float64)
+            m1 = s.reduce()[0]
+        res[storage] = {"mlups": round(float(n) ** 3 * steps / (ms / 1e3) / 1e6, 1),
+                        "mass_drift_rel": float((m1 - m0) / m0)}
+    ref = fields["f64"]
+    norm = np.sqrt((ref ** 2).sum())
+    for storage in ("f32", "f16s", "bf16s"):
+        d = fields[storage] - ref
+        res[storage]["l2_err_vs_f64"] = float(np.sqrt((d ** 2).sum()) / norm)
+        res[storage]["max_abs_err_vs_f64"] = float(np.abs(d).max())
+    res["f16s_speedup_vs_f32"] = round(res["f16s"]["mlups"] / res["f32"]["mlups"], 3)
+    return res
+
+
+def extensions(a):
+    """Bounded measurements of the batch and precision extensions, attached to
+    the benchmark line (full-size runs: --workload batch|precision)."""
+    out = {}
+    try:
+        out["batch_f32"] = batch_measure("f32", a.batch_count, 2000)
+        out["batch_f16s"] = batch_measure("f16s", a.batch_count, 2000)
+        out["batch_note"] = "batched MLUPS over the seeded 512-cavity workload; compare with single-domain MLUPS"
+    except Exception as e:  # keep the main line whatever happens here
+        out["batch_error"] = repr(e)
+    try:
+        out["precision"] = precision_measure(256, 1000)
+        out["precision_note"] = ("256^3, 1000 steps, lid 0.1, nu 0.0512 (the 512^3 / 5000-step configuration's "
+                                 "physics on a smaller grid; --workload precision runs the full size)")
+    except Exception as e:
+        out["precision_error"] = repr(e)
+    return out
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         reference_arm(a)
+        return
+    if a.workload == "batch":
+        import torch
+
+        torch.cuda.set_device(0)
+        res = {s: batch_measure(s, a.batch_count, a.batch_steps) for s in ("f32", "f16s")}
+        for s in ("f32", "f16s"):
+            res[s]["single_domain_384_mlups"] = round(single_measure(s, 384, 400), 1)
+            res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s]["single_domain_384_mlups"], 3)
+        print(json.dumps({"workload": "batch", "results": res}), flush=True)
+        return
+    if a.workload == "precision":
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"workload": "precision", "results": precision_measure(a.precision_size, a.precision_steps)}),
+              flush=True)
         return
     run_gpu(a)
 
@@ -365,12 +494,16 @@ def run_gpu(a):
         mlups, cores, kind, sample = cpu_run(a, a.cpu_seconds, use_reference=False)
         cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores, "kind": kind, "sample": sample}
 
+    ext = extensions(a) if (rank == 0 and world == 1 and not a.no_extensions) else None
+
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 5), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE_NAME[a.storage], "data": "synthetic",
                 "config": config_dict(a, world), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clocks.summary(), "gpu_launches": int(launches)}
+        if ext is not None:
+            line["extensions"] = ext
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist

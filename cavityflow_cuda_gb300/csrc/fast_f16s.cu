@@ -1,5 +1,5 @@
 // fast_f16s.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
-// step kernels for F16S storage (one translation unit per storage type, so
+// step kernels and the batch kernels for F16S storage (one translation unit per storage type, so
 // they compile in parallel).
 #include "lbm_fast.cuh"
 #include "lbm_kernels.h"
@@ -17,6 +17,12 @@ cudaError_t launch_tma_f16s(bool alpha, void* dd, const Grid& g, const Params& p
                           int consumer_warps, int* err, cudaStream_t st)
 {
     return launch_tma_impl<F16S>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
+}
+
+cudaError_t launch_batch_f16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                            long long vblocks, cudaStream_t st)
+{
+    return launch_batch_menu<F16S>(variant, alpha, pool, doms, ndom, vblocks, st);
 }
 
 }  // namespace lbm

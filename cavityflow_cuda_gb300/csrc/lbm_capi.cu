@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/lbm_gb300.h"
+#include "lbm_internal.h"
 #include "lbm_kernels.h"
 
 using lbm::Grid;
@@ -21,6 +22,10 @@ using lbm::Grid;
 namespace {
 
 thread_local char t_err[512] = "";
+
+}  // namespace
+
+namespace lbm_detail {
 
 int fail(int status, const char* fmt, ...)
 {
@@ -38,7 +43,9 @@ int cuda_fail(cudaError_t e, const char* what)
     return fail(LBM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
-}  // namespace
+}  // namespace lbm_detail
+
+using namespace lbm_detail;
 
 int lbm::record_error(int status, const char* fmt, ...)
 {
@@ -57,8 +64,12 @@ namespace {
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-int elem_bytes(int storage) { return storage == LBM_STORAGE_F64 ? 8 : storage == LBM_STORAGE_F32 ? 4 : 2; }
-int value_bytes(int storage) { return storage == LBM_STORAGE_F64 ? 8 : 4; }
+}  // namespace
+
+int lbm_detail::elem_bytes(int storage) { return storage == LBM_STORAGE_F64 ? 8 : storage == LBM_STORAGE_F32 ? 4 : 2; }
+int lbm_detail::value_bytes(int storage) { return storage == LBM_STORAGE_F64 ? 8 : 4; }
+
+namespace {
 
 bool valid_flag(int32_t f)
 {
@@ -71,60 +82,26 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // from autotuner measurements of the 384^3 cavity on GB300: 8-byte vectors
 // at two blocks per SM, except BF16, whose conversions favour 16-byte
 // vectors at one block per SM.
-int default_variant(int storage)
+}  // namespace
+
+int lbm_detail::default_variant(int storage)
 {
     return storage == LBM_STORAGE_BF16S ? 0 : 3;
 }
 
-// Cells per thread and block size of a variant (mirrors the menus of
-// lbm_fast.cuh and lbm_kernels.h).
-void variant_shape(int storage, int variant, int nx, int& cpt, int& block)
-{
-    static const int cpt_div[lbm::kRegisterVariants] = {1, 1, 1, 2, 2, 2, 4, 4};
-    static const int blocks[lbm::kRegisterVariants] = {256, 256, 128, 256, 256, 128, 256, 256};
-    if (variant >= lbm::kRegisterVariants) {
-        const lbm::TmaConfig c = lbm::kTmaMenu[variant - lbm::kRegisterVariants];
-        block = 32 * (1 + c.consumer_warps);
-        cpt = (c.rows * nx + 32 * c.consumer_warps - 1) / (32 * c.consumer_warps);
-        return;
-    }
-    const int V = 16 / (storage == LBM_STORAGE_F64 ? 8 : storage == LBM_STORAGE_F32 ? 4 : 2);
-    cpt = V / cpt_div[variant] > 0 ? V / cpt_div[variant] : 1;
-    block = blocks[variant];
-}
+namespace {
+
 
 }  // namespace
 
-struct lbm_solver {
-    Grid g{};
-    int storage = 0;
-    int device = 0;
-    lbm::Params p{};
-    int bc[6] = {0, 0, 0, 0, 0, 0};
-    void* dd = nullptr;             // populations, 19 * g.S elements
-    uint8_t* flags = nullptr;       // one byte per cell, reference layout
-    void* macros = nullptr;         // 4 * cells values (rho, jx, jy, jz)
-    bool macros_fresh = false;
-    double* scratch = nullptr;      // reduction partials (4 per block) + result (4)
-    unsigned long long* counts = nullptr;  // cavity-flag check counters [0..1], kernel error flag [2]
-    double* host_out = nullptr;     // pinned, 4 doubles
-    float* staging = nullptr;       // 16-bit storage: one packed slot cuboid
-    size_t staging_elems = 0;
-    int64_t counter = 0;
-    bool last_alpha = false;
-    int lid_y = -1;                 // fast path: lid row (ny) or 0 for none; -1: flag-array path
-    int variant = 0;                // launch variant of the vectorised kernels
-    cudaStream_t capture_stream = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    int64_t device_bytes = 0;
-};
 
-namespace {
 
-int* err_flag(lbm_solver* s) { return reinterpret_cast<int*>(s->counts + 2); }
+
+
+int* lbm_detail::err_flag(lbm_solver* s) { return reinterpret_cast<int*>(s->counts + 2); }
 
 // Reads and clears the kernels' timeout flag after the device is idle.
-int check_kernel_flag(lbm_solver* s)
+int lbm_detail::check_kernel_flag(lbm_solver* s)
 {
     int flag = 0;
     CK(cudaMemcpy(&flag, err_flag(s), sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy error flag");
@@ -134,6 +111,8 @@ int check_kernel_flag(lbm_solver* s)
     }
     return LBM_OK;
 }
+
+namespace {
 
 int check_solver(const lbm_solver* s)
 {
@@ -402,6 +381,13 @@ int lbm_derive_lattice(const lbm_physical* phys, int32_t storage, lbm_lattice* o
 
 int lbm_create(const lbm_params* prm, lbm_solver** out)
 {
+    return create_solver(prm, nullptr, out);
+}
+
+}  // extern "C"
+
+int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out)
+{
     if (!prm || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
     for (int d = 0; d < 3; ++d)
@@ -440,13 +426,18 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
     }
     s->variant = prm->fast_variant == 0 ? default_variant(s->storage) : prm->fast_variant - 1;
 
-    auto bail = [&](int r) { lbm_destroy(s); return r; };
+    auto bail = [&](int r) { destroy_solver(s); return r; };
     cudaError_t e = cudaSetDevice(s->device);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaSetDevice"));
     const size_t dd_bytes = (size_t)lbm::Q * s->g.S * elem_bytes(s->storage);
     const size_t flag_bytes = (size_t)s->g.cells();
     const size_t scratch_bytes = (4 * (size_t)lbm::kReduceMaxBlocks + 4) * sizeof(double);
-    if ((e = cudaMalloc(&s->dd, dd_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc populations"));
+    if (external_dd) {
+        s->dd = external_dd;
+        s->owns_dd = false;
+    } else if ((e = cudaMalloc(&s->dd, dd_bytes)) != cudaSuccess) {
+        return bail(cuda_fail(e, "cudaMalloc populations"));
+    }
     if ((e = cudaMalloc(&s->flags, flag_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc flags"));
     if ((e = cudaMalloc(&s->scratch, scratch_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc scratch"));
     if ((e = cudaMalloc(&s->counts, 4 * sizeof(unsigned long long))) != cudaSuccess)
@@ -457,7 +448,7 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
         return bail(cuda_fail(e, "cudaMallocHost"));
     if ((e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
         return bail(cuda_fail(e, "cudaStreamCreate"));
-    s->device_bytes = (int64_t)(dd_bytes + flag_bytes + scratch_bytes + 16);
+    s->device_bytes = (int64_t)((s->owns_dd ? dd_bytes : 0) + flag_bytes + scratch_bytes + 16);
 
     lbm::Bc bc;
     for (int f = 0; f < 6; ++f) bc.f[f] = prm->boundary[f];
@@ -473,14 +464,14 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
     return LBM_OK;
 }
 
-int lbm_destroy(lbm_solver* s)
+void lbm_detail::destroy_solver(lbm_solver* s)
 {
-    if (!s) return LBM_OK;
+    if (!s) return;
     cudaSetDevice(s->device);
     cudaDeviceSynchronize();
     drop_graph(s);
     if (s->capture_stream) cudaStreamDestroy(s->capture_stream);
-    if (s->dd) cudaFree(s->dd);
+    if (s->dd && s->owns_dd) cudaFree(s->dd);
     if (s->flags) cudaFree(s->flags);
     if (s->macros) cudaFree(s->macros);
     if (s->scratch) cudaFree(s->scratch);
@@ -488,6 +479,15 @@ int lbm_destroy(lbm_solver* s)
     if (s->staging) cudaFree(s->staging);
     if (s->host_out) cudaFreeHost(s->host_out);
     delete s;
+}
+
+extern "C" {
+
+int lbm_destroy(lbm_solver* s)
+{
+    if (!s) return LBM_OK;
+    if (s->batch) return fail(LBM_ERR_INVALID_ARGUMENT, "a batch domain is destroyed with its batch");
+    destroy_solver(s);
     return LBM_OK;
 }
 
@@ -505,7 +505,7 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     info->last_step_was_alpha = s->last_alpha ? 1 : 0;
     info->fast_path = s->lid_y >= 0 ? 1 : 0;
     info->fast_variant = s->variant;
-    variant_shape(s->storage, s->variant, s->g.nx, info->cells_per_thread, info->block_threads);
+    lbm::fast_variant_shape(s->storage, s->variant, s->g.nx, info->cells_per_thread, info->block_threads);
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;

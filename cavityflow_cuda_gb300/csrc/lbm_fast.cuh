@@ -329,3 +329,83 @@ cudaError_t launch_fast_menu(int variant, bool alpha, void* dd, const Grid& g, c
 }
 
 }  // namespace lbm
+
+namespace lbm {
+
+// ---------------------------------------------------------------------------
+// Batches: many box cavities advanced by one launch.  The domains' padded
+// population arrays share one device pool; a packed table gives each its
+// layout, offset, parameters and its range of "virtual blocks" (BLOCK
+// threads x CPT cells each, numbered consecutively over the domains).  A
+// persistent grid walks the virtual blocks; every CTA finds its domain by
+// binary search and runs the same per-thread bodies as the single-domain
+// kernels, so a domain's result does not depend on its neighbours in the
+// batch.
+// ---------------------------------------------------------------------------
+struct BatchDomain {
+    Grid g;
+    long long offset;       // elements from the pool base
+    double inv_tau;
+    double lid_u;
+    int lid_y;
+    long long block_start;  // first virtual block of this domain
+};
+
+template <class St, int CPT, int BLOCK, int MINB, bool kAlpha>
+__global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
+                                                          const BatchDomain* __restrict__ doms, const int ndom,
+                                                          const long long vblocks)
+{
+    using T = typename St::T;
+    for (long long vb = blockIdx.x; vb < vblocks; vb += gridDim.x) {
+        int lo = 0, hi = ndom - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (doms[mid].block_start <= vb) lo = mid;
+            else hi = mid - 1;
+        }
+        const BatchDomain d = doms[lo];
+        const long long t = (vb - d.block_start) * BLOCK + threadIdx.x;
+        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
+        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
+    }
+}
+
+template <class St, int VARIANT>
+cudaError_t launch_batch_variant(bool alpha, void* pool, const BatchDomain* doms, int ndom, long long vblocks,
+                                 cudaStream_t st)
+{
+    constexpr FastVariant fv = kFastMenu[VARIANT];
+    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div > 0
+                            ? (16 / (int)sizeof(typename St::bits)) / fv.cpt_div : 1;
+    auto kern = alpha ? batch_step<St, CPT, fv.block, fv.minb, true> : batch_step<St, CPT, fv.block, fv.minb, false>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, fv.block, 0);
+    if (e != cudaSuccess) return e;
+    long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms;
+    if (grid > vblocks) grid = vblocks;
+    if (grid < 1) return cudaSuccess;
+    kern<<<(int)grid, fv.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks);
+    return cudaGetLastError();
+}
+
+template <class St>
+cudaError_t launch_batch_menu(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                              long long vblocks, cudaStream_t st)
+{
+    switch (variant) {
+    case 0: return launch_batch_variant<St, 0>(alpha, pool, doms, ndom, vblocks, st);
+    case 1: return launch_batch_variant<St, 1>(alpha, pool, doms, ndom, vblocks, st);
+    case 2: return launch_batch_variant<St, 2>(alpha, pool, doms, ndom, vblocks, st);
+    case 3: return launch_batch_variant<St, 3>(alpha, pool, doms, ndom, vblocks, st);
+    case 4: return launch_batch_variant<St, 4>(alpha, pool, doms, ndom, vblocks, st);
+    case 5: return launch_batch_variant<St, 5>(alpha, pool, doms, ndom, vblocks, st);
+    case 6: return launch_batch_variant<St, 6>(alpha, pool, doms, ndom, vblocks, st);
+    case 7: return launch_batch_variant<St, 7>(alpha, pool, doms, ndom, vblocks, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace lbm

@@ -1,0 +1,53 @@
+// lbm_internal.h -- definitions shared by the C ABI translation units
+// (lbm_capi.cu, lbm_batch.cu); not part of the public interface.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_kernels.h"
+
+struct lbm_batch;
+
+struct lbm_solver {
+    lbm::Grid g{};
+    int storage = 0;
+    int device = 0;
+    lbm::Params p{};
+    int bc[6] = {0, 0, 0, 0, 0, 0};
+    void* dd = nullptr;             // populations, 19 * g.S elements
+    uint8_t* flags = nullptr;       // one byte per cell, reference layout
+    void* macros = nullptr;         // 4 * cells values (rho, jx, jy, jz)
+    bool macros_fresh = false;
+    double* scratch = nullptr;      // reduction partials (4 per block) + result (4)
+    unsigned long long* counts = nullptr;  // cavity-flag check counters [0..1], kernel error flag [2]
+    double* host_out = nullptr;     // pinned, 4 doubles
+    float* staging = nullptr;       // 16-bit storage: one packed slot cuboid
+    size_t staging_elems = 0;
+    int64_t counter = 0;
+    bool last_alpha = false;
+    int lid_y = -1;                 // fast path: lid row (ny) or 0 for none; -1: flag-array path
+    int variant = 0;                // launch variant of the vectorised kernels
+    cudaStream_t capture_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int64_t device_bytes = 0;
+    bool owns_dd = true;            // false: populations live in a batch's pool
+    lbm_batch* batch = nullptr;     // the batch this solver is a domain view of
+};
+
+namespace lbm_detail {
+
+int fail(int status, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+int elem_bytes(int storage);
+int value_bytes(int storage);
+int default_variant(int storage);
+// Creates a solver; with `external_dd` its populations live there (a batch
+// pool) and are initialised but never freed by the solver.
+int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out);
+void destroy_solver(lbm_solver* s);
+int* err_flag(lbm_solver* s);
+int check_kernel_flag(lbm_solver* s);
+
+}  // namespace lbm_detail

@@ -46,6 +46,21 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
                              int lid_y, int* err, cudaStream_t st);
 // Whether a variant fits this domain (shared memory of the bulk-copy kernels).
 bool fast_variant_fits(int storage, int variant, const Grid& g);
+// Cells per thread and threads per block of a variant (for a row of nx cells).
+void fast_variant_shape(int storage, int variant, int nx, int& cells_per_thread, int& block_threads);
+
+// Batches of box cavities (lbm_fast.cuh): register variants only.
+struct BatchDomain;
+cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                              long long vblocks, cudaStream_t st);
+cudaError_t launch_batch_f64(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                             long long vblocks, cudaStream_t st);
+cudaError_t launch_batch_f32(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                             long long vblocks, cudaStream_t st);
+cudaError_t launch_batch_f16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                              long long vblocks, cudaStream_t st);
+cudaError_t launch_batch_bf16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                               long long vblocks, cudaStream_t st);
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,

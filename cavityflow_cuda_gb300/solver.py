@@ -102,6 +102,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_get_densities": ([V, P, P, P], I),
         "lbm_set_densities": ([V, P, P, P], I),
         "lbm_reduce": ([V, P, P], I),
+        "lbm_batch_create": ([P, C.c_int32, C.c_int32, C.c_int32, P], I),
+        "lbm_batch_destroy": ([V], I),
+        "lbm_batch_get_info": ([V, P], I),
+        "lbm_batch_domain": ([V, C.c_int32, P], I),
+        "lbm_batch_run": ([V, I64, P], I),
+        "lbm_batch_set_fast_variant": ([V, C.c_int32], I),
+        "lbm_batch_autotune": ([V, C.c_int32, P, P], I),
         "lbm_status_string": ([I], C.c_char_p),
         "lbm_last_error": ([], C.c_char_p),
         "lbm_kernel_launches": ([], I64),
@@ -156,6 +163,17 @@ def derive_lattice(velocity=(0.05, 0.0, 0.0), acceleration=(0.0, 0.0, 0.0), visc
                 acceleration=tuple(out.acceleration), viscosity=out.viscosity)
 
 
+class _DomainSpec(C.Structure):
+    _fields_ = [("size", C.c_int32 * 3), ("reserved", C.c_int32), ("inv_tau", C.c_double),
+                ("lid_velocity", C.c_double)]
+
+
+class _BatchInfo(C.Structure):
+    _fields_ = [("count", C.c_int32), ("storage", C.c_int32), ("fast_variant", C.c_int32),
+                ("cells_per_thread", C.c_int32), ("block_threads", C.c_int32), ("reserved", C.c_int32),
+                ("interior_cells", C.c_int64), ("step_counter", C.c_int64), ("device_bytes", C.c_int64)]
+
+
 class CLbmSolverGB300:
     """One D3Q19 domain on one GPU, driven through the C ABI."""
 
@@ -181,8 +199,23 @@ class CLbmSolverGB300:
         if driven_cavity:
             self.setDrivenCavity()
 
+    @classmethod
+    def _view(cls, lib, handle, size, storage, owner):
+        """A non-owning wrapper of a batch domain's solver handle."""
+        self = cls.__new__(cls)
+        self._lib = lib
+        self._h = C.c_void_p(handle)
+        self._owner = owner
+        self.storage = storage
+        self.size = tuple(int(s) for s in size)
+        self.dtype = np.float64 if storage == "f64" else np.float32
+        return self
+
     # -- lifecycle --------------------------------------------------------
     def close(self) -> None:
+        if getattr(self, "_owner", None) is not None:
+            self._h = None
+            return
         if getattr(self, "_h", None):
             self._lib.lbm_destroy(self._h)
             self._h = None
@@ -319,3 +352,65 @@ class CLbmSolverGB300:
     def flags_all(self) -> np.ndarray:
         n = self.size
         return self.getFlags((0, 0, 0), (n[0] + 2, n[1] + 2, n[2] + 2))
+
+
+class LbmBatch:
+    """Many box cavities of uneven size and Reynolds number advanced together
+    by one persistent kernel per step (lbm_batch_* of include/lbm_gb300.h)."""
+
+    def __init__(self, domains, storage: str = "f32", device: int = 0):
+        """domains: iterable of (size(3), inv_tau, lid_velocity)."""
+        self._lib = load_library()
+        doms = list(domains)
+        arr = (_DomainSpec * len(doms))()
+        for i, (size, inv_tau, lid) in enumerate(doms):
+            arr[i].size[:] = [int(v) for v in size]
+            arr[i].inv_tau = float(inv_tau)
+            arr[i].lid_velocity = float(lid)
+        h = C.c_void_p()
+        _check(self._lib.lbm_batch_create(arr, len(doms), STORAGE[storage], int(device), C.byref(h)))
+        self._h = h
+        self.storage = storage
+        self.sizes = [tuple(int(v) for v in d[0]) for d in doms]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lbm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self) -> int:
+        return len(self.sizes)
+
+    def info(self) -> dict:
+        i = _BatchInfo()
+        _check(self._lib.lbm_batch_get_info(self._h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in _BatchInfo._fields_}
+
+    def domain(self, index: int) -> "CLbmSolverGB300":
+        v = C.c_void_p()
+        _check(self._lib.lbm_batch_domain(self._h, int(index), C.byref(v)))
+        return CLbmSolverGB300._view(self._lib, v.value, self.sizes[index], self.storage, self)
+
+    def run(self, steps: int, stream=None) -> None:
+        _check(self._lib.lbm_batch_run(self._h, int(steps), _stream_ptr(stream)))
+
+    def set_fast_variant(self, variant: int) -> None:
+        _check(self._lib.lbm_batch_set_fast_variant(self._h, int(variant)))
+
+    def autotune(self, pairs: int = 5):
+        ms = (C.c_float * 8)()
+        best = C.c_int32()
+        _check(self._lib.lbm_batch_autotune(self._h, int(pairs), C.byref(best), ms))
+        return best.value, list(ms)

@@ -285,6 +285,54 @@ int lbm_reduce(lbm_solver* solver, double out[4], void* stream);
 int lbm_reduce_noalloc(const void* populations, const int32_t* flags, const int32_t size[3], int32_t storage,
                        int32_t last_step_was_alpha, double* out_device, void* stream);
 
+/* ---- batches: many box cavities advanced together --------------------------
+ * No counterpart in the reference (one solver per MPI rank there).  Every
+ * domain is a lid-driven box cavity (obstacle halo, lid plane y = ny) with its
+ * own size, 1/tau and lid velocity; all advance the same time steps.  The
+ * populations of all domains share one device pool and one persistent kernel
+ * launch per step walks a packed table of the domains; long runs replay a
+ * CUDA graph.  A domain's results are bit-identical to the same domain run
+ * alone by an lbm_solver of the same storage. */
+typedef struct lbm_batch lbm_batch;   /* opaque */
+
+typedef struct lbm_domain_spec {
+    int32_t size[3];            /* interior cells                              */
+    int32_t reserved;           /* zero                                        */
+    double inv_tau;             /* 1/tau                                       */
+    double lid_velocity;        /* lid x velocity                              */
+} lbm_domain_spec;
+
+typedef struct lbm_batch_info {
+    int32_t count;              /* domains                                     */
+    int32_t storage;
+    int32_t fast_variant;       /* launch variant (register variants only)     */
+    int32_t cells_per_thread;
+    int32_t block_threads;
+    int32_t reserved;
+    int64_t interior_cells;     /* sum over domains: lattice updates per step  */
+    int64_t step_counter;
+    int64_t device_bytes;
+} lbm_batch_info;
+
+int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t storage, int32_t device,
+                     lbm_batch** out);
+/* Frees the batch and its domain views. */
+int lbm_batch_destroy(lbm_batch* batch);
+int lbm_batch_get_info(const lbm_batch* batch, lbm_batch_info* info);
+/* The solver handle of domain `index`: every single-domain getter, setter and
+ * lbm_reduce works on it.  Owned by the batch (lbm_destroy refuses it).  Do
+ * not step it alone: lbm_batch_run refuses a batch whose domains have left
+ * its time level. */
+int lbm_batch_domain(lbm_batch* batch, int32_t index, lbm_solver** view);
+/* `steps` steps of every domain (alpha on even counters, beta on odd). */
+int lbm_batch_run(lbm_batch* batch, int64_t steps, void* stream);
+/* Selects a launch variant (0..7, the register variants) for the batch kernel. */
+int lbm_batch_set_fast_variant(lbm_batch* batch, int32_t variant);
+/* Times each register variant on the whole batch (`pairs` alpha/beta pairs,
+ * CUDA events), keeps the fastest and restores the populations.  ms_per_pair
+ * (optional) receives 8 times.  Synchronous. */
+int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms_per_pair);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 const char* lbm_status_string(int status);
 /* Detail message of the last failing call on this thread ("" if none). */
