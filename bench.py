@@ -56,13 +56,15 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the CPU baseline sample")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch", "precision"],
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "batch", "precision", "serve"],
                     help="cavity: the single-domain benchmark line; batch / precision: the extension measurements")
     ap.add_argument("--no-extensions", action="store_true", help="skip the bounded extension measurements")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2000)
     ap.add_argument("--precision-size", type=int, default=512)
     ap.add_argument("--precision-steps", type=int, default=5000)
+    ap.add_argument("--serve-count", type=int, default=1000)
+    ap.add_argument("--serve-step-scale", type=float, default=0.05)
     return ap.parse_args()
 
 
@@ -344,6 +346,52 @@ def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
     return res
 
 
+def serve_measure(storage, count, step_scale, budget_gb=150.0, rate=200.0, seed=1, target_ms=50, device=0):
+    """p50/p99 latency and aggregate MLUPS of the seeded request stream (cube
+    edges {32..256} weighted, steps uniform in [500, 20000] times step_scale,
+    lid 0.05, Re log-uniform in [10, 5000], Poisson arrivals), replayed in
+    real time against a server with a budget_gb HBM budget."""
+    from cavityflow_cuda_gb300 import LbmServer
+    from cavityflow_cuda_gb300.workloads import serving_workload
+
+    reqs = serving_workload(count=count, seed=seed, rate=rate)
+    steps = [max(2, int(round(r.steps * step_scale))) for r in reqs]
+    lat, wait, lups = [], [], 0
+    with LbmServer(budget_bytes=int(budget_gb * 1e9), storage=storage, device=device, target_round_ms=target_ms,
+                   max_round_steps=512) as srv:
+        t0 = time.perf_counter()
+        i, hsub, ids, done, first_arrival, last_finish = 0, {}, {}, 0, None, 0.0
+        while done < count:
+            now = time.perf_counter() - t0
+            while i < count and reqs[i].arrival <= now:
+                rid = srv.submit(*reqs[i].solver_args(storage), steps[i])
+                ids[rid] = i
+                hsub[rid] = time.perf_counter() - t0
+                i += 1
+            ran = srv.round()
+            for c in srv.poll():
+                k = ids[c["id"]]
+                # finish - arrival, free of the offset between the two clocks
+                lat.append((c["finish_time"] - c["submit_time"]) + (hsub[c["id"]] - reqs[k].arrival))
+                wait.append(c["admit_time"] - c["submit_time"])
+                lups += c["cells"] * c["steps"]
+                last_finish = max(last_finish, hsub[c["id"]] + (c["finish_time"] - c["submit_time"]))
+                srv.take_result(c["id"], copy=False)
+                done += 1
+            if not ran and i < count:
+                time.sleep(max(0.0, min(0.005, reqs[i].arrival - (time.perf_counter() - t0))))
+        st = srv.stats()
+    span = last_finish - reqs[0].arrival
+    lat = np.array(lat)
+    return {"storage": storage, "requests": count, "step_scale": step_scale, "arrival_rate": rate,
+            "budget_gb": budget_gb, "p50_latency_s": round(float(np.percentile(lat, 50)), 3),
+            "p99_latency_s": round(float(np.percentile(lat, 99)), 3),
+            "p50_queue_wait_s": round(float(np.percentile(wait, 50)), 3),
+            "aggregate_mlups": round(lups / span / 1e6, 1), "busy_mlups": round(st["lattice_updates"] /
+                                                                               st["busy_seconds"] / 1e6, 1),
+            "makespan_s": round(span, 2), "rounds": st["rounds"], "peak_gb": round(st["peak_bytes"] / 1e9, 2)}
+
+
 def extensions(a):
     """Bounded measurements of the batch and precision extensions, attached to
     the benchmark line (full-size runs: --workload batch|precision)."""
@@ -354,6 +402,12 @@ def extensions(a):
         out["batch_note"] = "batched MLUPS over the seeded 512-cavity workload; compare with single-domain MLUPS"
     except Exception as e:  # keep the main line whatever happens here
         out["batch_error"] = repr(e)
+    try:
+        out["serve_f32"] = serve_measure("f32", 200, 0.02)
+        out["serve_note"] = ("first 200 requests of the seeded 10,000-request stream, steps scaled by 0.02; "
+                             "--workload serve runs larger samples")
+    except Exception as e:
+        out["serve_error"] = repr(e)
     try:
         out["precision"] = precision_measure(256, 1000)
         out["precision_note"] = ("256^3, 1000 steps, lid 0.1, nu 0.0512 (the 512^3 / 5000-step configuration's "
@@ -377,6 +431,13 @@ def main():
             res[s]["single_domain_384_mlups"] = round(single_measure(s, 384, 400), 1)
             res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s]["single_domain_384_mlups"], 3)
         print(json.dumps({"workload": "batch", "results": res}), flush=True)
+        return
+    if a.workload == "serve":
+        import torch
+
+        torch.cuda.set_device(0)
+        res = {s_: serve_measure(s_, a.serve_count, a.serve_step_scale) for s_ in ("f32", "f16s")}
+        print(json.dumps({"workload": "serve", "results": res}), flush=True)
         return
     if a.workload == "precision":
         import torch

@@ -5,11 +5,11 @@ include/lbm_gb300.h, implemented by hand-written sm_103a kernels in csrc/, and
 this Python binding of it (``CLbmSolverGB300``).
 """
 from .solver import (BACK, BOTTOM, DIRECTION_ALL, FLUID, FRONT, GHOST_LAYER, LEFT, OBSTACLE, RIGHT, STORAGE,
-                     TOP, VELOCITY_INJECTION, CLbmSolverGB300, LbmBatch, LbmError, declared_functions, derive_lattice,
+                     TOP, VELOCITY_INJECTION, CLbmSolverGB300, LbmBatch, LbmError, LbmServer, declared_functions, derive_lattice,
                      kernel_launches, load_library)
 
 __all__ = [
-    "CLbmSolverGB300", "LbmBatch", "LbmError", "derive_lattice", "declared_functions", "kernel_launches", "load_library",
+    "CLbmSolverGB300", "LbmBatch", "LbmError", "LbmServer", "derive_lattice", "declared_functions", "kernel_launches", "load_library",
     "OBSTACLE", "FLUID", "VELOCITY_INJECTION", "GHOST_LAYER", "DIRECTION_ALL", "LEFT", "RIGHT", "BOTTOM", "TOP",
     "BACK", "FRONT", "STORAGE",
 ]

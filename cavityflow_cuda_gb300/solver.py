@@ -109,6 +109,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_batch_run": ([V, I64, P], I),
         "lbm_batch_set_fast_variant": ([V, C.c_int32], I),
         "lbm_batch_autotune": ([V, C.c_int32, P, P], I),
+        "lbm_server_create": ([P, P], I),
+        "lbm_server_destroy": ([V], I),
+        "lbm_server_submit": ([V, P, P], I),
+        "lbm_server_round": ([V, P], I),
+        "lbm_server_poll": ([V, P, C.c_int32, P], I),
+        "lbm_server_take_result": ([V, C.c_int64, P, P], I),
+        "lbm_server_get_stats": ([V, P], I),
         "lbm_status_string": ([I], C.c_char_p),
         "lbm_last_error": ([], C.c_char_p),
         "lbm_kernel_launches": ([], I64),
@@ -414,3 +421,104 @@ class LbmBatch:
         best = C.c_int32()
         _check(self._lib.lbm_batch_autotune(self._h, int(pairs), C.byref(best), ms))
         return best.value, list(ms)
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("storage", C.c_int32), ("device", C.c_int32), ("max_round_steps", C.c_int32),
+                ("target_round_ms", C.c_int32), ("fast_variant", C.c_int32), ("reserved", C.c_int32),
+                ("budget_bytes", C.c_int64)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("size", C.c_int32 * 3), ("reserved", C.c_int32), ("inv_tau", C.c_double),
+                ("lid_velocity", C.c_double), ("steps", C.c_int64)]
+
+
+class _Completion(C.Structure):
+    _fields_ = [("id", C.c_int64), ("steps", C.c_int64), ("cells", C.c_int64), ("status", C.c_int32),
+                ("reserved", C.c_int32), ("submit_time", C.c_double), ("admit_time", C.c_double),
+                ("finish_time", C.c_double)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("queued", C.c_int64), ("active", C.c_int64), ("completed", C.c_int64),
+                ("bytes_in_use", C.c_int64), ("peak_bytes", C.c_int64), ("budget_bytes", C.c_int64),
+                ("lattice_updates", C.c_int64), ("rounds", C.c_int64), ("busy_seconds", C.c_double),
+                ("elapsed_seconds", C.c_double)]
+
+
+class LbmServer:
+    """Cavity-solve requests with continuous batching (lbm_server_* of
+    include/lbm_gb300.h)."""
+
+    def __init__(self, budget_bytes: int, storage: str = "f32", device: int = 0, max_round_steps: int = 256,
+                 target_round_ms: int = 50, fast_variant: int = -1):
+        self._lib = load_library()
+        cfg = _ServerConfig()
+        cfg.storage = STORAGE[storage]
+        cfg.device = int(device)
+        cfg.max_round_steps = int(max_round_steps)
+        cfg.target_round_ms = int(target_round_ms)
+        cfg.fast_variant = 0 if fast_variant < 0 else int(fast_variant) + 1
+        cfg.budget_bytes = int(budget_bytes)
+        h = C.c_void_p()
+        _check(self._lib.lbm_server_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.storage = storage
+        self.dtype = np.float64 if storage == "f64" else np.float32
+        self._sizes = {}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.lbm_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, size, inv_tau: float, lid_velocity: float, steps: int) -> int:
+        r = _Request()
+        r.size[:] = [int(v) for v in size]
+        r.inv_tau = float(inv_tau)
+        r.lid_velocity = float(lid_velocity)
+        r.steps = int(steps)
+        rid = C.c_int64()
+        _check(self._lib.lbm_server_submit(self._h, C.byref(r), C.byref(rid)))
+        self._sizes[rid.value] = tuple(int(v) for v in size)
+        return rid.value
+
+    def round(self) -> bool:
+        ran = C.c_int32()
+        _check(self._lib.lbm_server_round(self._h, C.byref(ran)))
+        return bool(ran.value)
+
+    def poll(self, capacity: int = 256) -> list:
+        buf = (_Completion * capacity)()
+        n = C.c_int32()
+        _check(self._lib.lbm_server_poll(self._h, buf, int(capacity), C.byref(n)))
+        return [{f: getattr(buf[i], f) for f, _ in _Completion._fields_} for i in range(n.value)]
+
+    def take_result(self, rid: int, copy: bool = True):
+        size = self._sizes.pop(rid)
+        if not copy:
+            status = self._lib.lbm_server_take_result(self._h, int(rid), None, None)
+            _check(status)
+            return None
+        rho = np.empty((size[2], size[1], size[0]), dtype=self.dtype)
+        u = np.empty((3, size[2], size[1], size[0]), dtype=self.dtype)
+        _check(self._lib.lbm_server_take_result(self._h, int(rid), rho.ctypes.data, u.ctypes.data))
+        return rho, u
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(self._lib.lbm_server_get_stats(self._h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in _ServerStats._fields_}

@@ -333,6 +333,70 @@ int lbm_batch_set_fast_variant(lbm_batch* batch, int32_t variant);
  * (optional) receives 8 times.  Synchronous. */
 int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms_per_pair);
 
+/* ---- servers: cavity-solve requests with continuous batching ---------------
+ * No counterpart in the reference.  Requests wait in FIFO order and are
+ * admitted while their populations fit a device arena sized to 95 % of the
+ * memory budget (the rest covers each request's flags and scratch).  Every
+ * round advances all resident requests together (the batch kernel over a
+ * packed table of them), sized to last about target_round_ms; finished
+ * requests copy density and velocity to host memory, free their memory and
+ * post a completion.  Requests that arrive while others run join the next
+ * round as memory frees up.  Each request's fields are bit-identical to the
+ * same cavity solved alone.  One host thread drives a server. */
+typedef struct lbm_server lbm_server;   /* opaque */
+
+typedef struct lbm_server_config {
+    int32_t storage;            /* lbm_storage of every request                */
+    int32_t device;
+    int32_t max_round_steps;    /* upper bound on steps per round (even)       */
+    int32_t target_round_ms;    /* rounds sized to about this long; 0: fixed   */
+    int32_t fast_variant;       /* 0: default; v + 1: register variant v       */
+    int32_t reserved;
+    int64_t budget_bytes;       /* device memory the server may hold           */
+} lbm_server_config;
+
+typedef struct lbm_request {
+    int32_t size[3];            /* interior cells of the box cavity            */
+    int32_t reserved;
+    double inv_tau;
+    double lid_velocity;
+    int64_t steps;
+} lbm_request;
+
+typedef struct lbm_completion {
+    int64_t id;
+    int64_t steps;
+    int64_t cells;              /* interior cells                              */
+    int32_t status;             /* LBM_OK or the error that ended the request  */
+    int32_t reserved;
+    double submit_time;         /* seconds since the server was created        */
+    double admit_time;
+    double finish_time;         /* result on the host                          */
+} lbm_completion;
+
+typedef struct lbm_server_stats {
+    int64_t queued, active, completed;
+    int64_t bytes_in_use, peak_bytes, budget_bytes;
+    int64_t lattice_updates;    /* interior-cell updates done so far           */
+    int64_t rounds;
+    double busy_seconds;        /* time spent in rounds                        */
+    double elapsed_seconds;     /* since creation                              */
+} lbm_server_stats;
+
+int lbm_server_create(const lbm_server_config* config, lbm_server** out);
+int lbm_server_destroy(lbm_server* server);
+/* Queues a request; LBM_ERR_BUDGET if it could never fit the budget. */
+int lbm_server_submit(lbm_server* server, const lbm_request* request, int64_t* id);
+/* Admits, runs one round and retires; *ran = 0 when nothing was resident. */
+int lbm_server_round(lbm_server* server, int32_t* ran);
+/* Moves up to `capacity` new completions to `out`. */
+int lbm_server_poll(lbm_server* server, lbm_completion* out, int32_t capacity, int32_t* count);
+/* Copies a finished request's interior density (nx*ny*nz values) and velocity
+ * (3 components) to the host buffers (either may be NULL) and releases it;
+ * returns the request's status. */
+int lbm_server_take_result(lbm_server* server, int64_t id, void* density, void* velocity);
+int lbm_server_get_stats(const lbm_server* server, lbm_server_stats* stats);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 const char* lbm_status_string(int status);
 /* Detail message of the last failing call on this thread ("" if none). */
