@@ -456,6 +456,20 @@ def barrier(world):
         dist.barrier()
 
 
+def combine_ranks(ms: float, units_per_rank: float, world: int, device=None):
+    """Whole-job throughput of independent replicas: the slowest rank's time
+    (all-reduce MAX) over the units all ranks processed.  Returns
+    (max_ms, units_per_second)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, units_per_rank * world / (ms / 1e3)
+
+
 def run_gpu(a):
     import torch
 
@@ -495,16 +509,9 @@ def run_gpu(a):
             ev1.synchronize()
         launches = kernel_launches() - l0
         torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1)
-        if world > 1:
-            import torch.distributed as dist
-
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms, lups_per_s = combine_ranks(ev0.elapsed_time(ev1), float(n) ** 3 * a.steps, world, device="cuda")
         barrier(world)
-        total_lups = float(n) ** 3 * a.steps * world
-        value = total_lups / (ms / 1e3) / 1e6
+        value = lups_per_s / 1e6
 
         # per-kernel durations (CUDA events on the launching stream)
         per = {"alpha": [], "beta": []}

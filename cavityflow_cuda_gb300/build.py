@@ -34,7 +34,8 @@ def _nvcc() -> str:
 
 
 def sources() -> list[str]:
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    """Library translation units: CUDA (.cu) and host C++ (.cpp), both through nvcc."""
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _stale(target: str, deps: list[str]) -> bool:
@@ -51,13 +52,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(os.path.dirname(PKG), "include", "lbm_gb300.h"))
     srcs = sources()
-    objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in srcs]
+    objs = [os.path.join(BUILD, os.path.basename(s).replace(".", "_") + ".o") for s in srcs]
 
     def compile_one(src_obj):
         src, obj = src_obj
         if not force and not _stale(obj, [src] + headers):
             return None
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        # .cpp units include the kernel headers, so they are compiled as CUDA too
+        lang = ["-x", "cu"] if src.endswith(".cpp") else []
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *lang, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -46,6 +46,20 @@ class _Lattice(C.Structure):
                 ("velocity", C.c_double * 3), ("acceleration", C.c_double * 3), ("viscosity", C.c_double)]
 
 
+class _Configuration(C.Structure):
+    _fields_ = [("velocity", C.c_double * 3), ("acceleration", C.c_double * 3), ("viscosity", C.c_double),
+                ("max_velocity", C.c_double), ("max_acceleration", C.c_double), ("domain_size", C.c_int32 * 3),
+                ("subdomain_num", C.c_int32 * 3), ("domain_length", C.c_double * 3),
+                ("cpu_subdomain_ratio", C.c_double), ("timestep", C.c_double), ("loops", C.c_int32),
+                ("do_benchmark", C.c_int32), ("do_logging", C.c_int32), ("do_validation", C.c_int32),
+                ("do_visualization", C.c_int32), ("visualization_rate", C.c_int32),
+                ("cpu_alpha_block", C.c_int32 * 3), ("cpu_beta_block", C.c_int32 * 3),
+                ("gpu_init_block", C.c_int32 * 3), ("gpu_alpha_block", C.c_int32 * 3),
+                ("gpu_beta_block", C.c_int32 * 3), ("reserved", C.c_int32), ("benchmark_dir", C.c_char * 256),
+                ("logging_dir", C.c_char * 256), ("validation_dir", C.c_char * 256),
+                ("visualization_dir", C.c_char * 256)]
+
+
 class _Params(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("boundary", C.c_int32 * 6),
                 ("inv_tau", C.c_double), ("lid_velocity", C.c_double), ("gravity", C.c_double * 3),
@@ -102,6 +116,12 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_get_densities": ([V, P, P, P], I),
         "lbm_set_densities": ([V, P, P, P], I),
         "lbm_reduce": ([V, P, P], I),
+        "lbm_read_configuration": ([C.c_char_p, P], I),
+        "lbm_configuration_physical": ([P, P], I),
+        "lbm_save_checkpoint": ([V, C.c_char_p], I),
+        "lbm_load_checkpoint": ([V, C.c_char_p], I),
+        "lbm_create_from_checkpoint": ([C.c_char_p, C.c_int32, P], I),
+        "lbm_write_vtk": ([V, C.c_char_p, P, C.c_int32], I),
         "lbm_batch_create": ([P, C.c_int32, C.c_int32, C.c_int32, P], I),
         "lbm_batch_destroy": ([V], I),
         "lbm_batch_get_info": ([V, P], I),
@@ -170,6 +190,37 @@ def derive_lattice(velocity=(0.05, 0.0, 0.0), acceleration=(0.0, 0.0, 0.0), visc
                 acceleration=tuple(out.acceleration), viscosity=out.viscosity)
 
 
+def read_configuration(path: str) -> dict:
+    """An XML configuration of the reference's schema, as
+    CConfiguration<T>::CConfiguration (src/CConfiguration.cpp:28-172) reads it."""
+    lib = load_library()
+    c = _Configuration()
+    _check(lib.lbm_read_configuration(os.fsencode(path), C.byref(c)))
+    out = {}
+    for f, t in _Configuration._fields_:
+        v = getattr(c, f)
+        if f.endswith("_dir"):
+            v = v.decode()
+        elif hasattr(t, "_length_"):
+            v = tuple(v)
+        out[f] = v
+    out.pop("reserved")
+    return out
+
+
+def configuration_lattice(path: str, storage: str = "f32") -> dict:
+    """Lattice parameters of an XML configuration (reader + derivation)."""
+    lib = load_library()
+    c = _Configuration()
+    _check(lib.lbm_read_configuration(os.fsencode(path), C.byref(c)))
+    ph = _Physical()
+    _check(lib.lbm_configuration_physical(C.byref(c), C.byref(ph)))
+    out = _Lattice()
+    _check(lib.lbm_derive_lattice(C.byref(ph), STORAGE[storage], C.byref(out)))
+    return dict(timestep=out.timestep, tau=out.tau, inv_tau=out.inv_tau, velocity=tuple(out.velocity),
+                acceleration=tuple(out.acceleration), viscosity=out.viscosity)
+
+
 class _DomainSpec(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("reserved", C.c_int32), ("inv_tau", C.c_double),
                 ("lid_velocity", C.c_double)]
@@ -216,6 +267,20 @@ class CLbmSolverGB300:
         self.storage = storage
         self.size = tuple(int(s) for s in size)
         self.dtype = np.float64 if storage == "f64" else np.float32
+        return self
+
+    @classmethod
+    def from_checkpoint(cls, path: str, device: int = 0) -> "CLbmSolverGB300":
+        """A solver restored from a checkpoint written by save_checkpoint."""
+        self = cls.__new__(cls)
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.lbm_create_from_checkpoint(os.fsencode(path), int(device), C.byref(h)))
+        self._h = h
+        i = self.info()
+        self.storage = {v: k for k, v in STORAGE.items()}[i["storage"]]
+        self.size = tuple(i["size"])
+        self.dtype = np.float64 if self.storage == "f64" else np.float32
         return self
 
     # -- lifecycle --------------------------------------------------------
@@ -284,6 +349,17 @@ class CLbmSolverGB300:
         best = C.c_int32()
         _check(self._lib.lbm_autotune(self._h, int(pairs), C.byref(best), ms))
         return best.value, list(ms)
+
+    # -- checkpoint and output --------------------------------------------
+    def save_checkpoint(self, path: str) -> None:
+        _check(self._lib.lbm_save_checkpoint(self._h, os.fsencode(path)))
+
+    def load_checkpoint(self, path: str) -> None:
+        _check(self._lib.lbm_load_checkpoint(self._h, os.fsencode(path)))
+
+    def write_vtk(self, path: str, length=None, binary: bool = False) -> None:
+        L = None if length is None else (C.c_double * 3)(*[float(v) for v in length])
+        _check(self._lib.lbm_write_vtk(self._h, os.fsencode(path), L, int(bool(binary))))
 
     # -- data -------------------------------------------------------------
     def _shape(self, size, comps):

@@ -108,6 +108,47 @@ typedef struct lbm_lattice {
  * constructor body of src/CLbmSolver.cpp:28-327. */
 int lbm_derive_lattice(const lbm_physical* phys, int32_t storage, lbm_lattice* out);
 
+/* The reference's XML configuration (configurations/*.xml), field for field
+ * (src/CConfiguration.hpp:57-104).  As in the reference built without MPI,
+ * subdomain-num is not read: subdomain_num is 1, 1, 1 and the domain is one
+ * subdomain on one GPU. */
+typedef struct lbm_configuration {
+    double velocity[3];
+    double acceleration[3];
+    double viscosity;
+    double max_velocity;
+    double max_acceleration;
+    int32_t domain_size[3];
+    int32_t subdomain_num[3];
+    double domain_length[3];
+    double cpu_subdomain_ratio;
+    double timestep;
+    int32_t loops;
+    int32_t do_benchmark;
+    int32_t do_logging;
+    int32_t do_validation;
+    int32_t do_visualization;
+    int32_t visualization_rate;
+    int32_t cpu_alpha_block[3];
+    int32_t cpu_beta_block[3];
+    int32_t gpu_init_block[3];
+    int32_t gpu_alpha_block[3];
+    int32_t gpu_beta_block[3];
+    int32_t reserved;
+    char benchmark_dir[256];
+    char logging_dir[256];
+    char validation_dir[256];
+    char visualization_dir[256];
+} lbm_configuration;
+
+/* Reads an XML configuration with the reference's schema.  Replaces
+ * CConfiguration<T>::CConfiguration (src/CConfiguration.cpp:28-172); its
+ * parameter checks (:174-197, asserts there) return LBM_ERR_CONFIG, a file
+ * that cannot be read LBM_ERR_IO. */
+int lbm_read_configuration(const char* path, lbm_configuration* out);
+/* The physical description lbm_derive_lattice takes, from a configuration. */
+int lbm_configuration_physical(const lbm_configuration* config, lbm_physical* out);
+
 /* Creation parameters of one solver. */
 typedef struct lbm_params {
     int32_t size[3];            /* interior cells nx, ny, nz (domain-size)     */
@@ -284,6 +325,26 @@ int lbm_reduce(lbm_solver* solver, double out[4], void* stream);
  * before any stream capture. */
 int lbm_reduce_noalloc(const void* populations, const int32_t* flags, const int32_t size[3], int32_t storage,
                        int32_t last_step_was_alpha, double* out_device, void* stream);
+
+/* ---- checkpoint and output ------------------------------------------------ */
+
+/* Writes the solver's whole state (parameters, flags, raw populations in the
+ * storage type, step counter and A-A parity) to `path` (through a temporary
+ * file renamed into place).  No counterpart in the reference, which cannot
+ * resume a run; a resumed run continues bit-identically. */
+int lbm_save_checkpoint(lbm_solver* solver, const char* path);
+/* Restores a checkpoint into a solver of the same size and storage. */
+int lbm_load_checkpoint(lbm_solver* solver, const char* path);
+/* Creates a solver on `device` from a checkpoint. */
+int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** out);
+
+/* Writes the interior as a legacy VTK structured grid: cell-corner points
+ * scaled to `length` (NULL: one unit per cell), then CELL_DATA flags,
+ * densities and velocities (double for F64 storage, float otherwise).  With
+ * binary = 0 the file is ASCII, as CLbmVisualizationVTK<T>::render
+ * (src/libvis/CLbmVisualizationVTK.cpp:69-205) writes it; binary = 1 writes
+ * the same records as legacy big-endian binary. */
+int lbm_write_vtk(lbm_solver* solver, const char* path, const double length[3], int32_t binary);
 
 /* ---- batches: many box cavities advanced together --------------------------
  * No counterpart in the reference (one solver per MPI rank there).  Every

@@ -189,6 +189,29 @@ class Oracle(_Lib):
         return np.array([fn(float(v)) for v in x.ravel()], dtype=np.uint16).reshape(x.shape)
 
     # -- convenience: the reference's time loop (src/CController.cpp:1278-1287) --
+    def config(self, xml_path: str, dtype) -> dict:
+        """Every field of the reference's XML reader (src/CConfiguration.cpp:28-172),
+        named as in include/lbm_gb300.h's lbm_configuration."""
+        r = np.zeros(14, dtype=np.float64)
+        n = np.zeros(27, dtype=np.int32)
+        dirs = C.create_string_buffer(4 * 256)
+        fn = self._fn("config", dtype)
+        fn.argtypes = [C.c_char_p, _P, _P, C.c_char_p]
+        fn(xml_path.encode(), _ptr(r), _ptr(n), dirs)
+        raw = dirs.raw
+        names = ["benchmark_dir", "logging_dir", "validation_dir", "visualization_dir"]
+        out = dict(velocity=tuple(r[0:3]), acceleration=tuple(r[3:6]), viscosity=r[6], max_velocity=r[7],
+                   max_acceleration=r[8], domain_length=tuple(r[9:12]), cpu_subdomain_ratio=r[12],
+                   timestep=r[13], domain_size=tuple(int(v) for v in n[0:3]),
+                   subdomain_num=tuple(int(v) for v in n[3:6]), loops=int(n[6]), do_benchmark=int(n[7]),
+                   do_logging=int(n[8]), do_validation=int(n[9]), do_visualization=int(n[10]),
+                   visualization_rate=int(n[11]), cpu_alpha_block=tuple(int(v) for v in n[12:15]),
+                   cpu_beta_block=tuple(int(v) for v in n[15:18]), gpu_init_block=tuple(int(v) for v in n[18:21]),
+                   gpu_alpha_block=tuple(int(v) for v in n[21:24]), gpu_beta_block=tuple(int(v) for v in n[24:27]))
+        for i, name in enumerate(names):
+            out[name] = raw[256 * i:256 * (i + 1)].split(b"\0", 1)[0].decode()
+        return out
+
     def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):
         if counter & 1:
             self.beta(dd, flags, inv_tau, lid_u)
@@ -238,6 +261,29 @@ class Reference(_Lib):
         fn = self._fn("params", dtype)
         fn.argtypes = [C.c_char_p, _P]
         fn(xml_path.encode(), _ptr(out))
+        return out
+
+    def config(self, xml_path: str, dtype) -> dict:
+        """Every field of the reference's XML reader (src/CConfiguration.cpp:28-172),
+        named as in include/lbm_gb300.h's lbm_configuration."""
+        r = np.zeros(14, dtype=np.float64)
+        n = np.zeros(27, dtype=np.int32)
+        dirs = C.create_string_buffer(4 * 256)
+        fn = self._fn("config", dtype)
+        fn.argtypes = [C.c_char_p, _P, _P, C.c_char_p]
+        fn(xml_path.encode(), _ptr(r), _ptr(n), dirs)
+        raw = dirs.raw
+        names = ["benchmark_dir", "logging_dir", "validation_dir", "visualization_dir"]
+        out = dict(velocity=tuple(r[0:3]), acceleration=tuple(r[3:6]), viscosity=r[6], max_velocity=r[7],
+                   max_acceleration=r[8], domain_length=tuple(r[9:12]), cpu_subdomain_ratio=r[12],
+                   timestep=r[13], domain_size=tuple(int(v) for v in n[0:3]),
+                   subdomain_num=tuple(int(v) for v in n[3:6]), loops=int(n[6]), do_benchmark=int(n[7]),
+                   do_logging=int(n[8]), do_validation=int(n[9]), do_visualization=int(n[10]),
+                   visualization_rate=int(n[11]), cpu_alpha_block=tuple(int(v) for v in n[12:15]),
+                   cpu_beta_block=tuple(int(v) for v in n[15:18]), gpu_init_block=tuple(int(v) for v in n[18:21]),
+                   gpu_alpha_block=tuple(int(v) for v in n[21:24]), gpu_beta_block=tuple(int(v) for v in n[24:27]))
+        for i, name in enumerate(names):
+            out[name] = raw[256 * i:256 * (i + 1)].split(b"\0", 1)[0].decode()
         return out
 
     def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):

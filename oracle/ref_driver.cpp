@@ -116,9 +116,48 @@ void ref_params(const char* xml, double out[10])
     probe.dump(out);
 }
 
+// Every field of the reference's configuration reader
+// (src/CConfiguration.hpp:57-96): 14 reals, 27 integers, 4 directories of
+// 256 bytes each.
+template <class T>
+void ref_config(const char* xml, double* r, int32_t* n, char* dirs)
+{
+    CConfiguration<T> c{std::string(xml)};
+    const T reals[14] = {c.velocity[0], c.velocity[1], c.velocity[2], c.acceleration[0], c.acceleration[1],
+                         c.acceleration[2], c.viscosity, c.maxVelocityDimLess, c.maxAccelerationDimLess,
+                         c.domainLength[0], c.domainLength[1], c.domainLength[2], c.CPUSubdomainRatio, c.timestep};
+    for (int i = 0; i < 14; ++i) r[i] = (double)reals[i];
+    int k = 0;
+    for (int d = 0; d < 3; ++d) n[k++] = c.domainSize[d];
+    for (int d = 0; d < 3; ++d) n[k++] = c.numOfSubdomains[d];
+    n[k++] = c.loops;
+    n[k++] = c.doBenchmark;
+    n[k++] = c.doLogging;
+    n[k++] = c.doValidation;
+    n[k++] = c.doVisualization;
+    n[k++] = c.visualizationRate;
+    for (int b = 0; b < 2; ++b)
+        for (int d = 0; d < 3; ++d) n[k++] = c.elementsPerBlock[b][d];
+    for (int b = 0; b < 3; ++b) {
+        n[k++] = (int32_t)c.threadsPerBlock[b].x;
+        n[k++] = (int32_t)c.threadsPerBlock[b].y;
+        n[k++] = (int32_t)c.threadsPerBlock[b].z;
+    }
+    const std::string* ds[4] = {&c.benchmarkOutputDir, &c.loggingOutputDir, &c.validationOutputDir,
+                                &c.visualizationOutputDir};
+    for (int i = 0; i < 4; ++i) {
+        const size_t m = ds[i]->size() < 255 ? ds[i]->size() : 255;
+        ds[i]->copy(dirs + 256 * i, m);
+        dirs[256 * i + m] = 0;
+    }
+}
+
 }  // namespace
 
 extern "C" {
+
+void ref_config_d(const char* xml, double* r, int32_t* n, char* dirs) { ref_config<double>(xml, r, n, dirs); }
+void ref_config_f(const char* xml, double* r, int32_t* n, char* dirs) { ref_config<float>(xml, r, n, dirs); }
 
 void ref_params_d(const char* xml, double out[10]) { ref_params<double>(xml, out); }
 void ref_params_f(const char* xml, double out[10]) { ref_params<float>(xml, out); }

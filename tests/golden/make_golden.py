@@ -116,6 +116,73 @@ CONFIGS = {
 }
 
 
+# A configuration that sets every field of the reader to a non-default value,
+# with comments and loose whitespace, for the reader's own parity test.
+READER_VARIETY = """<?xml version="1.0" encoding="ISO-8859-1"?>
+<!-- every field non-default -->
+<lbm-configuration>
+  <physics>
+    <velocity>
+      <x> 0.075 </x><y>0.001</y><z>-0.002</z>
+    </velocity>
+    <acceleration><x>0.0001</x><y>-0.0002</y><z>0.0003</z></acceleration>
+    <viscosity>0.0425</viscosity>
+    <max-velocity>0.09</max-velocity>
+    <max-acceleration>0.05</max-acceleration>
+  </physics>
+  <grid>
+    <domain-size><x>40</x><y>24</y><z>32</z></domain-size>
+    <!-- the reference's own spelling of this tag -->
+    <domian-length><x>40</x><y>24</y><z>32</z></domian-length>
+    <subdomain-num><x>2</x><y>1</y><z>1</z></subdomain-num>
+    <cpu-subdomain-ratio>0.25</cpu-subdomain-ratio>
+  </grid>
+  <simulation>
+    <loops>123</loops>
+    <timestep>1.0</timestep>
+    <benchmark><do>1</do><output-dir>out/bench</output-dir></benchmark>
+    <logging><do>1</do><output-dir>out/log</output-dir></logging>
+    <validation><do>1</do><output-dir>out/valid</output-dir></validation>
+    <visualization><do>1</do><rate>7</rate><output-dir>out/vis</output-dir></visualization>
+  </simulation>
+  <cpu>
+    <block-configuration>
+      <alpha-block-configuration><x>16</x><y>8</y><z>4</z></alpha-block-configuration>
+      <beta-block-configuration><x>8</x><y>4</y><z>2</z></beta-block-configuration>
+    </block-configuration>
+  </cpu>
+  <gpu>
+    <grid-configuration>
+      <init-grid-configuration><x>64</x><y>4</y><z>2</z></init-grid-configuration>
+      <alpha-grid-configuration><x>128</x><y>2</y><z>1</z></alpha-grid-configuration>
+      <beta-grid-configuration><x>256</x><y>1</y><z>1</z></beta-grid-configuration>
+    </grid-configuration>
+  </gpu>
+</lbm-configuration>
+"""
+
+
+def make_config_fixtures() -> None:
+    """configs.json: every field the reference's reader returns for each
+    configs/*.xml, in double and in float; each read runs in its own process
+    because the reference's checks assert."""
+    cfg_dir = os.path.join(HERE, "configs")
+    with open(os.path.join(cfg_dir, "reader_variety.xml"), "w") as fh:
+        fh.write(READER_VARIETY)
+    out = {}
+    for f in sorted(os.listdir(cfg_dir)):
+        if not f.endswith(".xml"):
+            continue
+        out[f[:-4]] = {}
+        for tag in ("f64", "f32"):
+            r = subprocess.run([sys.executable, __file__, "--config-one", os.path.join(cfg_dir, f), tag],
+                               capture_output=True, text=True)
+            out[f[:-4]][tag] = ({"error": True} if r.returncode != 0
+                                else json.loads(r.stdout.strip().splitlines()[-1]))
+    with open(os.path.join(HERE, "configs.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 def post_collision(dd: np.ndarray, last_was_alpha: bool) -> np.ndarray:
     """Interior post-collision populations f_k (19, nz, ny, nx): after alpha
     they sit swapped in the cell's own slots, after beta in slot k of x + c_k."""
@@ -154,7 +221,17 @@ def main() -> None:
     ap.add_argument("--ref-src", default="/root/reference/src")
     ap.add_argument("--skip-digests", action="store_true")
     ap.add_argument("--params-one", nargs=2, metavar=("XML", "DTYPE"))
+    ap.add_argument("--config-one", nargs=2, metavar=("XML", "DTYPE"))
+    ap.add_argument("--configs-only", action="store_true", help="regenerate configs.json only")
     args = ap.parse_args()
+    if args.config_one:
+        xml, tag = args.config_one
+        print(json.dumps(orc.Reference().config(xml, np.float64 if tag == "f64" else np.float32)))
+        return
+    if args.configs_only:
+        orc.build(args.ref_src)
+        make_config_fixtures()
+        return
     if args.params_one:
         xml, tag = args.params_one
         v = orc.Reference().params(xml, np.float64 if tag == "f64" else np.float32)
@@ -185,6 +262,7 @@ def main() -> None:
                     ["timestep", "tau", "tau_inv", "ux", "uy", "uz", "gx", "gy", "gz", "nu"], v))
     with open(os.path.join(HERE, "params.json"), "w") as fh:
         json.dump(params, fh, indent=1, sort_keys=True)
+    make_config_fixtures()
 
     # 2. small cases: full arrays
     for name, nx, ny, nz, dtype, nu, U, steps_list, g, lid in SMALL_CASES:
