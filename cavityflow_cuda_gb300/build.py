@@ -2,7 +2,8 @@
 
 ``python -m cavityflow_cuda_gb300.build`` (or ``build()``) compiles every
 ``csrc/*.cu`` translation unit in parallel with nvcc and links
-``cavityflow_cuda_gb300/liblbm_gb300.so``.  Object files go to
+``cavityflow_cuda_gb300/liblbm_gb300.so`` and the ``lbm_gb300`` command
+beside it (host/lbm_main.cpp).  Object files go to
 ``cavityflow_cuda_gb300/_build/`` (git-ignored).
 
 The library is compiled with ``-fmad=false``: the FP64/FP32 collision must
@@ -21,6 +22,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "liblbm_gb300.so")
+HOST = os.path.join(PKG, "host")
+CLI = os.path.join(PKG, "lbm_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -76,7 +79,25 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(LIB + ".tmp", LIB)
+    build_cli(verbose, force)
     return LIB
+
+
+def build_cli(verbose: bool = False, force: bool = False) -> str:
+    """Link the lbm_gb300 command (host C++ over the C ABI) beside the library."""
+    src = os.path.join(HOST, "lbm_main.cpp")
+    header = os.path.join(os.path.dirname(PKG), "include", "lbm_gb300.h")
+    if force or _stale(CLI, [src, header, LIB]):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", CLI + ".tmp", f"-L{PKG}", "-llbm_gb300",
+               "-Wl,-rpath,$ORIGIN"]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"building lbm_gb300 failed:\n{r.stdout}\n{r.stderr}")
+        os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

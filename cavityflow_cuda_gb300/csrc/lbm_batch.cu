@@ -39,7 +39,7 @@ struct lbm_batch {
     std::vector<lbm_solver*> views;
     std::vector<lbm::BatchDomain> table;
     lbm::BatchDomain* dtable = nullptr;
-    long long vblocks = 0;
+    long long vblocks[2] = {0, 0};  // virtual blocks of the alpha and the beta kernel
     long long interior_cells = 0;
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -60,16 +60,18 @@ void drop_batch_graph(lbm_batch* b)
 // Numbers the virtual blocks of the current variant and uploads the table.
 int build_table(lbm_batch* b)
 {
-    long long next = 0;
-    for (size_t i = 0; i < b->views.size(); ++i) {
-        lbm::BatchDomain& d = b->table[i];
-        int cpt = 1, block = 1;
-        lbm::fast_variant_shape(b->storage, b->variant, d.g.nx, cpt, block);
-        const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
-        d.block_start = next;
-        next += (groups + block - 1) / block;
+    for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
+        long long next = 0;
+        for (size_t i = 0; i < b->views.size(); ++i) {
+            lbm::BatchDomain& d = b->table[i];
+            int cpt = 1, block = 1;
+            lbm::fast_variant_shape(b->storage, b->variant, kind == 0, d.g.nx, cpt, block);
+            const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
+            d.block_start[kind] = next;
+            next += (groups + block - 1) / block;
+        }
+        b->vblocks[kind] = next;
     }
-    b->vblocks = next;
     CK(cudaMemcpy(b->dtable, b->table.data(), b->table.size() * sizeof(lbm::BatchDomain), cudaMemcpyHostToDevice),
        "cudaMemcpy batch table");
     drop_batch_graph(b);
@@ -78,8 +80,8 @@ int build_table(lbm_batch* b)
 
 cudaError_t batch_launch(lbm_batch* b, int variant, bool alpha, cudaStream_t st)
 {
-    return lbm::launch_batch_step(b->storage, variant, alpha, b->pool, b->dtable, (int)b->views.size(), b->vblocks,
-                                  st);
+    return lbm::launch_batch_step(b->storage, variant, alpha, b->pool, b->dtable, (int)b->views.size(),
+                                  b->vblocks[alpha ? 0 : 1], st);
 }
 
 void sync_views(lbm_batch* b)
@@ -197,7 +199,8 @@ int lbm_batch_get_info(const lbm_batch* b, lbm_batch_info* info)
     info->count = (int32_t)b->views.size();
     info->storage = b->storage;
     info->fast_variant = b->variant;
-    lbm::fast_variant_shape(b->storage, b->variant, 1, info->cells_per_thread, info->block_threads);
+    lbm::fast_variant_shape(b->storage, b->variant, true, 1, info->cells_per_thread, info->block_threads);
+    lbm::fast_variant_shape(b->storage, b->variant, false, 1, info->beta_cells_per_thread, info->beta_block_threads);
     info->interior_cells = b->interior_cells;
     info->step_counter = b->counter;
     int64_t bytes = (int64_t)b->pool_bytes + (int64_t)(b->table.size() * sizeof(lbm::BatchDomain));

@@ -78,15 +78,21 @@ bool valid_flag(int32_t f)
 
 constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 
-// Default launch variant per storage (index into the menu of lbm_fast.cuh),
-// from autotuner measurements of the 384^3 cavity on GB300: 8-byte vectors
-// at two blocks per SM, except BF16, whose conversions favour 16-byte
-// vectors at one block per SM.
+// Default launch variant per storage (index into kFastMenu), from kernel
+// timings of the 384^3 cavity on GB300: two-warp blocks with the block-wide
+// beta exchange; FP32 with 8-byte vectors in both kernels, FP16 with a 16-byte
+// alpha and an 8-byte beta, BF16 with 16-byte vectors in both.  FP64 is bound
+// by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
 }  // namespace
 
 int lbm_detail::default_variant(int storage)
 {
-    return storage == LBM_STORAGE_BF16S ? 0 : 3;
+    switch (storage) {
+    case LBM_STORAGE_F32: return 8;
+    case LBM_STORAGE_F16S: return 10;
+    case LBM_STORAGE_BF16S: return 11;
+    default: return 3;
+    }
 }
 
 namespace {
@@ -505,7 +511,9 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     info->last_step_was_alpha = s->last_alpha ? 1 : 0;
     info->fast_path = s->lid_y >= 0 ? 1 : 0;
     info->fast_variant = s->variant;
-    lbm::fast_variant_shape(s->storage, s->variant, s->g.nx, info->cells_per_thread, info->block_threads);
+    lbm::fast_variant_shape(s->storage, s->variant, true, s->g.nx, info->cells_per_thread, info->block_threads);
+    lbm::fast_variant_shape(s->storage, s->variant, false, s->g.nx, info->beta_cells_per_thread,
+                            info->beta_block_threads);
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;

@@ -14,16 +14,23 @@
 //                  crosses into the next thread's group is exchanged with
 //                  warp shuffles, and only lanes at a warp or row edge touch
 //                  that element with a scalar access.
+//   beta_fast_blk -- the same step with the exchange widened to the whole
+//                  block (shuffles inside a warp, shared memory between
+//                  warps), so that only the block's two end lanes and row
+//                  edges use scalar accesses.
 //
 // Template parameters: St storage type, CPT cells per thread (one vector of
-// CPT elements per slot: 16 or 8 bytes), BLOCK threads per block, MINB the
-// minimum resident blocks per SM requested from the register allocator.
+// CPT elements per slot: 16, 8 or 4 bytes), BLOCK threads per block, MINB the
+// minimum resident blocks per SM requested from the register allocator.  The
+// launch menu (kFastMenu, lbm_kernels.h) picks them per kernel.
 #pragma once
 
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 
 #include "lbm_core.cuh"
+#include "lbm_kernels.h"
 
 namespace lbm {
 
@@ -268,6 +275,171 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     });
 }
 
+// Beta step with the neighbour exchange done block-wide: inside a warp by
+// shuffles, across the warps of a block through shared memory (two block
+// barriers), so only lanes at a row edge or at the block's two ends touch the
+// odd element with a scalar access; every other thread issues exactly 19
+// vector loads and 19 vector stores, as in alpha.  All BLOCK threads of the
+// block must call it together, with consecutive t.
+template <class St, int CPT, int BLOCK>
+__device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ dd, const Grid& g,
+                                               const typename St::T inv_tau, const typename St::T lid_u,
+                                               const int lid_y, const long long t)
+{
+    using T = typename St::T;
+    using bits = typename St::bits;
+    using IO = Vio<St, CPT>;
+    constexpr int W = BLOCK / 32;
+    // [warp][k >> 1] for the ten slots k < 12 with c_x != 0: the first and last
+    // element of a warp's vectors before the collision (s_first, s_last) and
+    // after it (s_head, s_tail).
+    __shared__ bits s_first[W][6], s_last[W][6], s_head[W][6], s_tail[W][6];
+    const int G = (g.nx + CPT - 1) / CPT;
+    const long long total = (long long)G * g.ny * g.nz;
+    const bool active = t < total;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const long long tt = active ? t : 0;  // inactive lanes read a valid cell, never write
+    const int gi = (int)(tt % G);
+    const long long row = tt / G;
+    const int y = 1 + (int)(row % g.ny);
+    const int z = 1 + (int)(row / g.ny);
+    const int x0 = 1 + gi * CPT;
+    // The neighbouring group of the same row belongs to thread t -+ 1 of this block.
+    const bool left_in = gi > 0 && threadIdx.x > 0;
+    const bool right_in = gi < G - 1 && threadIdx.x < BLOCK - 1;
+
+    bits a[Q][CPT];
+    bits ext[Q];  // the odd element fetched by a scalar load at a block or row edge
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        IO::load_raw(dd + rb, a[k]);
+        ext[k] = bits(0);
+        if constexpr (cx == 1) {
+            if (active && !right_in) ext[k] = dd[rb + CPT];
+        } else if constexpr (cx == -1) {
+            if (active && !left_in) ext[k] = dd[rb - 1];
+        }
+    });
+    // warp-edge lanes publish the elements the neighbouring warps need
+    static_for<0, 12>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        if constexpr (dir_x(k) == 1) {
+            if (lane == 0) s_first[warp][k >> 1] = a[k][0];
+        } else if constexpr (dir_x(k) == -1) {
+            if (lane == 31) s_last[warp][k >> 1] = a[k][CPT - 1];
+        }
+    });
+    __syncthreads();
+
+    // p[k][v]: value of slot k at (cell x0+v) + c_k; edge[k]: the aligned
+    // element outside the shifted window, rewritten unchanged at a row edge.
+    bits p[Q][CPT];
+    bits edge[Q];
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        if constexpr (cx == 0) {
+#pragma unroll
+            for (int v = 0; v < CPT; ++v) p[k][v] = a[k][v];
+            edge[k] = bits(0);
+        } else if constexpr (cx == 1) {
+            bits nb = shfl_down_bits(a[k][0], 1);
+            if (lane == 31 && warp < W - 1) nb = s_first[warp + 1][k >> 1];
+            if (!right_in) nb = ext[k];
+#pragma unroll
+            for (int v = 0; v < CPT - 1; ++v) p[k][v] = a[k][v + 1];
+            p[k][CPT - 1] = nb;
+            edge[k] = a[k][0];
+        } else {
+            bits pb = shfl_up_bits(a[k][CPT - 1], 1);
+            if (lane == 0 && warp > 0) pb = s_last[warp - 1][k >> 1];
+            if (!left_in) pb = ext[k];
+            p[k][0] = pb;
+#pragma unroll
+            for (int v = 1; v < CPT; ++v) p[k][v] = a[k][v - 1];
+            edge[k] = a[k][CPT - 1];
+        }
+    });
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+#pragma unroll
+    for (int v = 0; v < CPT; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
+        T c[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load(p[k][v]);
+        if (lid) inject(c, rho0, lid_u);
+        else collide<St>(c, inv_tau);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) p[k][v] = St::store(c[k]);  // population k -> slot k at x + c_k
+    }
+
+    static_for<0, 12>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        if constexpr (dir_x(k) == 1) {
+            if (lane == 31) s_tail[warp][k >> 1] = p[k][CPT - 1];
+        } else if constexpr (dir_x(k) == -1) {
+            if (lane == 0) s_head[warp][k >> 1] = p[k][0];
+        }
+    });
+    __syncthreads();
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        if constexpr (cx == 0) {
+            if (active) IO::store_raw(dd + rb, p[k]);
+        } else if constexpr (cx == 1) {
+            // aligned element 0 belongs to cell x0-1 (thread t-1)
+            bits from_left = shfl_up_bits(p[k][CPT - 1], 1);
+            if (lane == 0 && warp > 0) from_left = s_tail[warp - 1][k >> 1];
+            if (active) {
+                bits o[CPT];
+#pragma unroll
+                for (int v = 1; v < CPT; ++v) o[v] = p[k][v - 1];
+                if (left_in || gi == 0) {
+                    o[0] = left_in ? from_left : edge[k];
+                    IO::store_raw(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 1; v < CPT; ++v) dd[rb + v] = o[v];
+                }
+                if (!right_in && x0 + CPT - 1 <= g.nx) dd[rb + CPT] = p[k][CPT - 1];
+            }
+        } else {
+            // aligned element CPT-1 belongs to cell x0+CPT (thread t+1)
+            bits from_right = shfl_down_bits(p[k][0], 1);
+            if (lane == 31 && warp < W - 1) from_right = s_head[warp + 1][k >> 1];
+            if (active) {
+                bits o[CPT];
+#pragma unroll
+                for (int v = 0; v < CPT - 1; ++v) o[v] = p[k][v + 1];
+                if (right_in || gi == G - 1) {
+                    o[CPT - 1] = right_in ? from_right : edge[k];
+                    IO::store_raw(dd + rb, o);
+                } else {
+#pragma unroll
+                    for (int v = 0; v < CPT - 1; ++v) dd[rb + v] = o[v];
+                }
+                if (!left_in) dd[rb - 1] = p[k][0];
+            }
+        }
+    });
+}
+
+template <class St, int CPT, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) beta_fast_blk(typename St::bits* __restrict__ dd, const Grid g,
+                                                             const typename St::T inv_tau,
+                                                             const typename St::T lid_u, const int lid_y)
+{
+    beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
+}
+
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                          const typename St::T inv_tau,
@@ -276,56 +448,54 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __re
     beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
 }
 
-// Launch menu shared by every storage type: (cells per thread as a fraction
-// of a 16-byte vector, block size, minimum blocks per SM).  Index = variant.
-struct FastVariant {
-    int cpt_div;   // cells per thread = (16 bytes / element) / cpt_div
-    int block;
-    int minb;
-};
-constexpr int kFastVariants = 8;
-constexpr FastVariant kFastMenu[kFastVariants] = {
-    {1, 256, 1},  // 16-byte vectors, registers unconstrained
-    {1, 256, 2},  // 16-byte vectors, <= 128 registers
-    {1, 128, 4},  // 16-byte vectors, <= 128 registers, smaller blocks
-    {2, 256, 2},  // 8-byte vectors, <= 128 registers
-    {2, 256, 3},  // 8-byte vectors, <= 85 registers
-    {2, 128, 5},  // 8-byte vectors, <= 102 registers
-    {4, 256, 2},  // 4-byte vectors (FP64: one cell), <= 128 registers
-    {4, 256, 3},  // 4-byte vectors (FP64: one cell), <= 85 registers
-};
+// Cells per thread of a kernel shape for storage St (at least one).
+template <class St>
+constexpr int shape_cpt(const KernelShape& k)
+{
+    return (16 / (int)sizeof(typename St::bits)) / k.cpt_div > 0 ? (16 / (int)sizeof(typename St::bits)) / k.cpt_div
+                                                                  : 1;
+}
 
 template <class St, int VARIANT>
 cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, cudaStream_t st)
 {
     using T = typename St::T;
     constexpr FastVariant fv = kFastMenu[VARIANT];
-    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div > 0
-                            ? (16 / (int)sizeof(typename St::bits)) / fv.cpt_div : 1;
-    const int G = (g.nx + CPT - 1) / CPT;
-    const long long threads = (long long)G * g.ny * g.nz;
-    const int blocks = (int)((threads + fv.block - 1) / fv.block);
     auto* d = static_cast<typename St::bits*>(dd);
-    if (alpha) alpha_fast<St, CPT, fv.block, fv.minb><<<blocks, fv.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
-    else beta_fast<St, CPT, fv.block, fv.minb><<<blocks, fv.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+    if (alpha) {
+        constexpr KernelShape k = fv.alpha;
+        constexpr int CPT = shape_cpt<St>(k);
+        const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
+        const int blocks = (int)((threads + k.block - 1) / k.block);
+        alpha_fast<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+    } else {
+        constexpr KernelShape k = fv.beta;
+        constexpr int CPT = shape_cpt<St>(k);
+        const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
+        const int blocks = (int)((threads + k.block - 1) / k.block);
+        if constexpr (fv.block_exchange)
+            beta_fast_blk<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+        else
+            beta_fast<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+    }
     return cudaGetLastError();
+}
+
+template <class St, size_t... I>
+cudaError_t launch_fast_table(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                              cudaStream_t st, std::index_sequence<I...>)
+{
+    using Fn = cudaError_t (*)(bool, void*, const Grid&, const Params&, int, cudaStream_t);
+    static constexpr Fn table[] = {&launch_fast_variant<St, (int)I>...};
+    return table[variant](alpha, dd, g, p, lid_y, st);
 }
 
 template <class St>
 cudaError_t launch_fast_menu(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                              cudaStream_t st)
 {
-    switch (variant) {
-    case 0: return launch_fast_variant<St, 0>(alpha, dd, g, p, lid_y, st);
-    case 1: return launch_fast_variant<St, 1>(alpha, dd, g, p, lid_y, st);
-    case 2: return launch_fast_variant<St, 2>(alpha, dd, g, p, lid_y, st);
-    case 3: return launch_fast_variant<St, 3>(alpha, dd, g, p, lid_y, st);
-    case 4: return launch_fast_variant<St, 4>(alpha, dd, g, p, lid_y, st);
-    case 5: return launch_fast_variant<St, 5>(alpha, dd, g, p, lid_y, st);
-    case 6: return launch_fast_variant<St, 6>(alpha, dd, g, p, lid_y, st);
-    case 7: return launch_fast_variant<St, 7>(alpha, dd, g, p, lid_y, st);
-    default: return cudaErrorInvalidValue;
-    }
+    if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
+    return launch_fast_table<St>(variant, alpha, dd, g, p, lid_y, st, std::make_index_sequence<kRegisterVariants>{});
 }
 
 }  // namespace lbm
@@ -348,64 +518,78 @@ struct BatchDomain {
     double inv_tau;
     double lid_u;
     int lid_y;
-    long long block_start;  // first virtual block of this domain
+    long long block_start[2];  // first virtual block of this domain: [0] alpha, [1] beta kernel
 };
 
-template <class St, int CPT, int BLOCK, int MINB, bool kAlpha>
+template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, bool kExchange>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
                                                           const BatchDomain* __restrict__ doms, const int ndom,
                                                           const long long vblocks)
 {
     using T = typename St::T;
+    constexpr int which = kAlpha ? 0 : 1;
+    // Every thread of a CTA walks the same virtual blocks, so the block-wide
+    // barriers of the exchanging beta body are reached uniformly.
     for (long long vb = blockIdx.x; vb < vblocks; vb += gridDim.x) {
         int lo = 0, hi = ndom - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (doms[mid].block_start <= vb) lo = mid;
+            if (doms[mid].block_start[which] <= vb) lo = mid;
             else hi = mid - 1;
         }
         const BatchDomain d = doms[lo];
-        const long long t = (vb - d.block_start) * BLOCK + threadIdx.x;
+        const long long t = (vb - d.block_start[which]) * BLOCK + threadIdx.x;
         if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
+        else if constexpr (kExchange)
+            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
         else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
     }
+}
+
+template <class St, int VARIANT, bool kAlpha>
+cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, long long vblocks, cudaStream_t st)
+{
+    constexpr FastVariant fv = kFastMenu[VARIANT];
+    constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
+    constexpr int CPT = shape_cpt<St>(k);
+    auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha, fv.block_exchange>;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, k.block, 0);
+    if (e != cudaSuccess) return e;
+    long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms;
+    if (grid > vblocks) grid = vblocks;
+    if (grid < 1) return cudaSuccess;
+    kern<<<(int)grid, k.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks);
+    return cudaGetLastError();
 }
 
 template <class St, int VARIANT>
 cudaError_t launch_batch_variant(bool alpha, void* pool, const BatchDomain* doms, int ndom, long long vblocks,
                                  cudaStream_t st)
 {
-    constexpr FastVariant fv = kFastMenu[VARIANT];
-    constexpr int CPT = (16 / (int)sizeof(typename St::bits)) / fv.cpt_div > 0
-                            ? (16 / (int)sizeof(typename St::bits)) / fv.cpt_div : 1;
-    auto kern = alpha ? batch_step<St, CPT, fv.block, fv.minb, true> : batch_step<St, CPT, fv.block, fv.minb, false>;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, fv.block, 0);
-    if (e != cudaSuccess) return e;
-    long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms;
-    if (grid > vblocks) grid = vblocks;
-    if (grid < 1) return cudaSuccess;
-    kern<<<(int)grid, fv.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks);
-    return cudaGetLastError();
+    return alpha ? launch_batch_kernel<St, VARIANT, true>(pool, doms, ndom, vblocks, st)
+                 : launch_batch_kernel<St, VARIANT, false>(pool, doms, ndom, vblocks, st);
 }
 
+template <class St, size_t... I>
+cudaError_t launch_batch_table(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                               long long vblocks, cudaStream_t st, std::index_sequence<I...>)
+{
+    using Fn = cudaError_t (*)(bool, void*, const BatchDomain*, int, long long, cudaStream_t);
+    static constexpr Fn table[] = {&launch_batch_variant<St, (int)I>...};
+    return table[variant](alpha, pool, doms, ndom, vblocks, st);
+}
+
+// `vblocks`: the virtual blocks of the kernel launched (alpha or beta shape).
 template <class St>
 cudaError_t launch_batch_menu(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
                               long long vblocks, cudaStream_t st)
 {
-    switch (variant) {
-    case 0: return launch_batch_variant<St, 0>(alpha, pool, doms, ndom, vblocks, st);
-    case 1: return launch_batch_variant<St, 1>(alpha, pool, doms, ndom, vblocks, st);
-    case 2: return launch_batch_variant<St, 2>(alpha, pool, doms, ndom, vblocks, st);
-    case 3: return launch_batch_variant<St, 3>(alpha, pool, doms, ndom, vblocks, st);
-    case 4: return launch_batch_variant<St, 4>(alpha, pool, doms, ndom, vblocks, st);
-    case 5: return launch_batch_variant<St, 5>(alpha, pool, doms, ndom, vblocks, st);
-    case 6: return launch_batch_variant<St, 6>(alpha, pool, doms, ndom, vblocks, st);
-    case 7: return launch_batch_variant<St, 7>(alpha, pool, doms, ndom, vblocks, st);
-    default: return cudaErrorInvalidValue;
-    }
+    if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
+    return launch_batch_table<St>(variant, alpha, pool, doms, ndom, vblocks, st,
+                                  std::make_index_sequence<kRegisterVariants>{});
 }
 
 }  // namespace lbm

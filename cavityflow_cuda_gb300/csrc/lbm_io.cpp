@@ -261,12 +261,18 @@ int lbm_write_vtk(lbm_solver* s, const char* path, const double length[3], int32
     auto sep = [&](char c) {
         if (!binary) std::fputc(c, f);
     };
+    // (origin + i) * length / size in the value type, as the reference
+    // computes the corner coordinates (origin 0: one subdomain)
+    auto corner = [&](int i, int d, int n) -> double {
+        if (dbl) return (double)i * L[d] / (double)n;
+        return (double)((float)i * (float)L[d] / (float)n);
+    };
     for (int k = 0; k <= nz; ++k)
         for (int j = 0; j <= ny; ++j)
             for (int i = 0; i <= nx; ++i) {
-                put(i * L[0] / nx); sep(' ');
-                put(j * L[1] / ny); sep(' ');
-                put(k * L[2] / nz); sep('\n');
+                put(corner(i, 0, nx)); sep(' ');
+                put(corner(j, 1, ny)); sep(' ');
+                put(corner(k, 2, nz)); sep('\n');
             }
     if (binary) std::fputc('\n', f);
     std::fprintf(f, "CELL_DATA %lld\nSCALARS flags INT 1\nLOOKUP_TABLE default\n", (long long)n);

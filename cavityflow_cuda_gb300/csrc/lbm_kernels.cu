@@ -384,19 +384,18 @@ bool fast_variant_fits(int storage, int variant, const Grid& g)
     return (size_t)c.stages * stage + 2 * (size_t)c.stages * sizeof(uint64_t) + 16 + 1024 <= (size_t)max_optin;
 }
 
-void fast_variant_shape(int storage, int variant, int nx, int& cpt, int& block)
+void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, int& block)
 {
-    static const int cpt_div[kRegisterVariants] = {1, 1, 1, 2, 2, 2, 4, 4};
-    static const int blocks[kRegisterVariants] = {256, 256, 128, 256, 256, 128, 256, 256};
     if (variant >= kRegisterVariants) {
         const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
         block = 32 * (1 + c.consumer_warps);
         cpt = (c.rows * nx + 32 * c.consumer_warps - 1) / (32 * c.consumer_warps);
         return;
     }
+    const KernelShape k = alpha ? kFastMenu[variant].alpha : kFastMenu[variant].beta;
     const int V = 16 / (storage == 0 ? 8 : storage == 1 ? 4 : 2);
-    cpt = V / cpt_div[variant] > 0 ? V / cpt_div[variant] : 1;
-    block = blocks[variant];
+    cpt = V / k.cpt_div > 0 ? V / k.cpt_div : 1;
+    block = k.block;
 }
 
 cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,

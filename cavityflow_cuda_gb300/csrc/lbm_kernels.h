@@ -26,12 +26,46 @@ void add_launches(long long n);
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
 cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
-// Box-cavity step.  Variants 0..kRegisterVariants-1 index the register
-// kernels of lbm_fast.cuh (cells per thread, block size, blocks per SM); the
-// rest index kTmaMenu, the row-pipelined bulk-copy kernels of lbm_tma.cuh.
-// A variant that does not fit the domain returns cudaErrorInvalidValue
-// before launching anything.  `err` receives the bulk-copy kernels' timeout flag.
-constexpr int kRegisterVariants = 8;
+// Box-cavity step.  Variants 0..kRegisterVariants-1 index kFastMenu, the
+// register kernels of lbm_fast.cuh; the rest index kTmaMenu, the
+// row-pipelined bulk-copy kernels of lbm_tma.cuh.  A variant that does not
+// fit the domain returns cudaErrorInvalidValue before launching anything.
+// `err` receives the bulk-copy kernels' timeout flag.
+//
+// Launch shape of one register kernel: cells per thread as a fraction of a
+// 16-byte vector (cpt_div 1: 16-byte vectors, 2: 8-byte, 4: 4-byte), threads
+// per block, and the minimum resident blocks per SM requested from the
+// register allocator (65536 / (block * minb) registers per thread at most).
+struct KernelShape {
+    int cpt_div;
+    int block;
+    int minb;
+};
+// A register variant: the alpha and the beta kernel have their own shapes
+// (the population layout does not depend on them), and the beta kernel
+// exchanges the odd element of its shifted slots either inside each warp
+// (shuffles; warp-edge lanes use scalar accesses) or across the whole block
+// (shuffles plus shared memory; only block- and row-edge lanes do).
+struct FastVariant {
+    KernelShape alpha;
+    KernelShape beta;
+    bool block_exchange;
+};
+constexpr int kRegisterVariants = 12;
+constexpr FastVariant kFastMenu[kRegisterVariants] = {
+    {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
+    {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
+    {{1, 128, 4}, {1, 128, 4}, false},  // 16-byte vectors, <= 128 registers, smaller blocks
+    {{2, 256, 2}, {2, 256, 2}, false},  // 8-byte vectors, <= 128 registers
+    {{2, 256, 3}, {2, 256, 3}, false},  // 8-byte vectors, <= 85 registers
+    {{2, 128, 5}, {2, 128, 5}, false},  // 8-byte vectors, <= 102 registers
+    {{4, 256, 2}, {4, 256, 2}, false},  // 4-byte vectors (FP64: one cell), <= 128 registers
+    {{4, 256, 3}, {4, 256, 3}, false},  // 4-byte vectors (FP64: one cell), <= 85 registers
+    {{2, 64, 8}, {2, 64, 8}, true},     // 8-byte vectors, two-warp blocks, block exchange
+    {{2, 128, 4}, {2, 128, 4}, true},   // 8-byte vectors, four-warp blocks, block exchange
+    {{1, 64, 4}, {2, 64, 8}, true},     // alpha 16-byte, beta 8-byte vectors, block exchange
+    {{1, 64, 4}, {1, 64, 4}, true},     // 16-byte vectors, two-warp blocks, block exchange
+};
 struct TmaConfig {
     int rows;            // rows per work unit
     int stages;          // shared-memory buffers
@@ -46,8 +80,9 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
                              int lid_y, int* err, cudaStream_t st);
 // Whether a variant fits this domain (shared memory of the bulk-copy kernels).
 bool fast_variant_fits(int storage, int variant, const Grid& g);
-// Cells per thread and threads per block of a variant (for a row of nx cells).
-void fast_variant_shape(int storage, int variant, int nx, int& cells_per_thread, int& block_threads);
+// Cells per thread and threads per block of a variant's alpha or beta kernel
+// (for a row of nx cells).
+void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cells_per_thread, int& block_threads);
 
 // Batches of box cavities (lbm_fast.cuh): register variants only.
 struct BatchDomain;

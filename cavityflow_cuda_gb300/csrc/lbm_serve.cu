@@ -213,10 +213,10 @@ int admit(lbm_server* s)
 }
 
 // Packs the given requests into the device table for `variant`.
-int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long& vblocks)
+int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&vblocks)[2])
 {
     s->table.resize(reqs.size());
-    long long next = 0;
+    long long next[2] = {0, 0};
     for (size_t i = 0; i < reqs.size(); ++i) {
         const lbm_solver* v = reqs[i]->view;
         lbm::BatchDomain& d = s->table[i];
@@ -226,13 +226,16 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long& vb
         d.inv_tau = v->p.inv_tau;
         d.lid_u = v->p.lid_u;
         d.lid_y = v->g.ny;
-        int cpt = 1, block = 1;
-        lbm::fast_variant_shape(s->cfg.storage, s->variant, d.g.nx, cpt, block);
-        const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
-        d.block_start = next;
-        next += (groups + block - 1) / block;
+        for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
+            int cpt = 1, block = 1;
+            lbm::fast_variant_shape(s->cfg.storage, s->variant, kind == 0, d.g.nx, cpt, block);
+            const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
+            d.block_start[kind] = next[kind];
+            next[kind] += (groups + block - 1) / block;
+        }
     }
-    vblocks = next;
+    vblocks[0] = next[0];
+    vblocks[1] = next[1];
     if (reqs.size() > s->dtable_cap) {
         if (s->dtable) cudaFree(s->dtable);
         s->dtable = nullptr;
@@ -392,12 +395,12 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     }
     long long run_cells = 0;
     for (Request* r : run) run_cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
-    long long vblocks = 0;
+    long long vblocks[2] = {0, 0};
     if (int rc = upload_table(s, run, vblocks)) return rc;
     const auto t_start = std::chrono::steady_clock::now();
     for (int64_t i = 0; i < q; ++i)
         CK(lbm::launch_batch_step(s->cfg.storage, s->variant, (i & 1) == 0, s->arena, s->dtable, (int)run.size(),
-                                  vblocks, s->stream),
+                                  vblocks[i & 1], s->stream),
            "server step launch");
     CK(cudaStreamSynchronize(s->stream), "server round");
     const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();

@@ -70,7 +70,8 @@ class _Info(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("value_size", C.c_int32),
                 ("vector_cells", C.c_int32), ("step_counter", C.c_int64), ("last_step_was_alpha", C.c_int32),
                 ("fast_path", C.c_int32), ("fast_variant", C.c_int32), ("cells_per_thread", C.c_int32),
-                ("block_threads", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
+                ("block_threads", C.c_int32), ("beta_cells_per_thread", C.c_int32),
+                ("beta_block_threads", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
                 ("device_bytes", C.c_int64)]
 
 
@@ -228,7 +229,8 @@ class _DomainSpec(C.Structure):
 
 class _BatchInfo(C.Structure):
     _fields_ = [("count", C.c_int32), ("storage", C.c_int32), ("fast_variant", C.c_int32),
-                ("cells_per_thread", C.c_int32), ("block_threads", C.c_int32), ("reserved", C.c_int32),
+                ("cells_per_thread", C.c_int32), ("block_threads", C.c_int32),
+                ("beta_cells_per_thread", C.c_int32), ("beta_block_threads", C.c_int32), ("reserved", C.c_int32),
                 ("interior_cells", C.c_int64), ("step_counter", C.c_int64), ("device_bytes", C.c_int64)]
 
 
@@ -493,7 +495,7 @@ class LbmBatch:
         _check(self._lib.lbm_batch_set_fast_variant(self._h, int(variant)))
 
     def autotune(self, pairs: int = 5):
-        ms = (C.c_float * 8)()
+        ms = (C.c_float * 12)()
         best = C.c_int32()
         _check(self._lib.lbm_batch_autotune(self._h, int(pairs), C.byref(best), ms))
         return best.value, list(ms)

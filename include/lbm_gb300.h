@@ -180,8 +180,10 @@ typedef struct lbm_info {
     int32_t fast_path;          /* 1: flags match the box cavity, so the
                                    vectorised kernels run; 0: flag-array path  */
     int32_t fast_variant;       /* launch variant of the vectorised kernels    */
-    int32_t cells_per_thread;   /* cells per thread of that variant            */
-    int32_t block_threads;      /* threads per block of that variant           */
+    int32_t cells_per_thread;   /* cells per thread of its alpha kernel        */
+    int32_t block_threads;      /* threads per block of its alpha kernel       */
+    int32_t beta_cells_per_thread;  /* the same for its beta kernel            */
+    int32_t beta_block_threads;
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */
@@ -244,9 +246,11 @@ int lbm_synchronize(lbm_solver* solver);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: register-blocked
- * vector kernels (cells per thread, threads per block, blocks per SM) and
- * row-pipelined bulk-copy kernels (rows per unit, buffers, consumer warps). */
+/* Number of launch variants of the box-cavity kernels: 12 register-blocked
+ * vector kernels (0..11: cells per thread, threads per block and blocks per
+ * SM of the alpha and the beta kernel, and whether beta exchanges edge
+ * elements per warp or per block) and 6 row-pipelined bulk-copy kernels
+ * (12..17: rows per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Selects a variant for subsequent steps; LBM_ERR_UNSUPPORTED if it needs more
  * shared memory than this domain allows. */
@@ -367,8 +371,10 @@ typedef struct lbm_batch_info {
     int32_t count;              /* domains                                     */
     int32_t storage;
     int32_t fast_variant;       /* launch variant (register variants only)     */
-    int32_t cells_per_thread;
+    int32_t cells_per_thread;   /* alpha kernel                                */
     int32_t block_threads;
+    int32_t beta_cells_per_thread;  /* beta kernel                             */
+    int32_t beta_block_threads;
     int32_t reserved;
     int64_t interior_cells;     /* sum over domains: lattice updates per step  */
     int64_t step_counter;
@@ -387,11 +393,11 @@ int lbm_batch_get_info(const lbm_batch* batch, lbm_batch_info* info);
 int lbm_batch_domain(lbm_batch* batch, int32_t index, lbm_solver** view);
 /* `steps` steps of every domain (alpha on even counters, beta on odd). */
 int lbm_batch_run(lbm_batch* batch, int64_t steps, void* stream);
-/* Selects a launch variant (0..7, the register variants) for the batch kernel. */
+/* Selects a launch variant (0..11, the register variants) for the batch kernel. */
 int lbm_batch_set_fast_variant(lbm_batch* batch, int32_t variant);
 /* Times each register variant on the whole batch (`pairs` alpha/beta pairs,
  * CUDA events), keeps the fastest and restores the populations.  ms_per_pair
- * (optional) receives 8 times.  Synchronous. */
+ * (optional) receives 12 times.  Synchronous. */
 int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms_per_pair);
 
 /* ---- servers: cavity-solve requests with continuous batching ---------------

@@ -18,7 +18,9 @@ WORKER = textwrap.dedent("""
     dist.init_process_group("gloo")
     rank, world = dist.get_rank(), dist.get_world_size()
     ms, ups = bench.combine_ranks(100.0 * (rank + 1), 1000.0, world, device="cpu")
-    print(json.dumps({{"rank": rank, "ms": ms, "ups": ups}}), flush=True)
+    # one file per rank: the launcher may interleave the ranks' stdout
+    with open(os.path.join({out!r}, f"rank{{rank}}.json"), "w") as fh:
+        fh.write(json.dumps({{"rank": rank, "ms": ms, "ups": ups}}))
     dist.destroy_process_group()
 """)
 
@@ -34,10 +36,10 @@ def test_replicas_take_the_slowest_rank(tmp_path):
     import json
 
     script = tmp_path / "worker.py"
-    script.write_text(WORKER.format(root=ROOT))
+    script.write_text(WORKER.format(root=ROOT, out=str(tmp_path)))
     r = _torchrun(str(script))
     assert r.returncode == 0, r.stderr[-2000:]
-    lines = [json.loads(l) for l in r.stdout.splitlines() if l.startswith("{")]
+    lines = [json.loads(open(tmp_path / f"rank{i}.json").read()) for i in range(2)]
     assert len(lines) == 2
     for d in lines:
         assert d["ms"] == 200.0                      # max over ranks

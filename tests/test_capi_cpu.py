@@ -87,3 +87,33 @@ def test_header_cites_reference_for_each_replaced_entry_point():
         i = text.index(sym + "(")
         block = text[max(0, i - 700):i]
         assert "src/" in block, sym
+
+
+def test_cli_usage_and_argument_errors(lib, tmp_path):
+    """The lbm_gb300 command parses its arguments and reads the configuration
+    before it touches a GPU; errors exit 1 as the reference's exit(EXIT_FAILURE)."""
+    import subprocess
+
+    from cavityflow_cuda_gb300 import build
+
+    cli = build.CLI
+    assert os.access(cli, os.X_OK)
+    r = subprocess.run([cli, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "usage: lbm_gb300" in r.stderr
+    cfg = os.path.join(GOLDEN, "configs", "cavity64_re100.xml")
+    for args in ([], [cfg, cfg], [cfg, "--storage", "f8"], [cfg, "--bogus"], [cfg, "--checkpoint-every", "5"],
+                 [str(tmp_path / "absent.xml")], [os.path.join(GOLDEN, "configs", "infeasible.xml")]):
+        r = subprocess.run([cli, *args], capture_output=True, text=True)
+        assert r.returncode == 1 and r.stderr.startswith("usage") or "lbm_gb300:" in r.stderr, (args, r.stderr)
+        assert r.returncode == 1, args
+    import torch
+
+    if not torch.cuda.is_available():
+        r = subprocess.run([cli, cfg], capture_output=True, text=True)
+        assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+def test_launch_variant_menu_size(lib):
+    """12 register variants (0-11) and 6 bulk-copy variants (12-17); the GPU
+    parity tests enumerate exactly these."""
+    assert lib.lbm_fast_variant_count() == 18
