@@ -7,7 +7,7 @@ counters, beta on odd, as src/CController.cpp:1278-1287 alternates them);
 MLUPS counts interior cells x steps (src/CController.cpp:1463-1464).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--storage f32|f64|f16s|bf16s] [--size 384]
+                    [--storage f32|f64|f16s|bf16s|f16sr] [--size 384]
 
 Prints ONE JSON line (rank 0).  Keys beyond the base contract:
   roofline      -- dominant kernel's algorithmic bytes / CUDA-event time vs
@@ -37,8 +37,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_VALUE = {"f64": 8, "f32": 4, "f16s": 2, "bf16s": 2}
-DTYPE_NAME = {"f64": "f64", "f32": "f32", "f16s": "f16 (shifted, fp32 collide)", "bf16s": "bf16 (shifted, fp32 collide)"}
+BYTES_PER_VALUE = {"f64": 8, "f32": 4, "f16s": 2, "bf16s": 2, "f16sr": 2}
+DTYPE_NAME = {"f64": "f64", "f32": "f32", "f16s": "f16 (shifted, fp32 collide)", "bf16s": "bf16 (shifted, fp32 collide)",
+              "f16sr": "f16 (shifted, scaled 2^12, stochastic rounding, fp32 collide)"}
 METRIC = "MLUPS"
 L2_BYTES = 129 * 1024 * 1024
 
@@ -320,7 +321,7 @@ def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
 
     res = {"domain": [n] * 3, "steps": steps, "lid": lid, "nu": nu, "re": round(n * lid / nu, 1)}
     fields = {}
-    for storage in ("f64", "f32", "f16s", "bf16s"):
+    for storage in ("f64", "f32", "f16s", "bf16s", "f16sr"):
         _, inv_tau = lattice_tau(nu, storage)
         T = np.float64 if storage == "f64" else np.float32
         stream = torch.cuda.Stream()
@@ -338,11 +339,12 @@ def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
                         "mass_drift_rel": float((m1 - m0) / m0)}
     ref = fields["f64"]
     norm = np.sqrt((ref ** 2).sum())
-    for storage in ("f32", "f16s", "bf16s"):
+    for storage in ("f32", "f16s", "bf16s", "f16sr"):
         d = fields[storage] - ref
         res[storage]["l2_err_vs_f64"] = float(np.sqrt((d ** 2).sum()) / norm)
         res[storage]["max_abs_err_vs_f64"] = float(np.abs(d).max())
     res["f16s_speedup_vs_f32"] = round(res["f16s"]["mlups"] / res["f32"]["mlups"], 3)
+    res["f16sr_speedup_vs_f32"] = round(res["f16sr"]["mlups"] / res["f32"]["mlups"], 3)
     return res
 
 
@@ -528,9 +530,14 @@ def run_gpu(a):
         peak, peak_kind = measured_peaks()
         algo = bytes_per_lup * float(n) ** 3
         achieved = algo / (avg[dom] / 1e3) / 1e9
-        traffic = profile_traffic(a, f"{dom}_fast")
+        info = s.info()
+        kname = f"{dom}_fast" + ("_blk" if dom == "beta" and info["beta_block_exchange"] else "")
+        if info["fast_variant"] >= 12:
+            kname = "step_tma"
+        traffic = profile_traffic(a, kname)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"{dom}_fast<{a.storage}>",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": f"{kname}<{a.storage}>",
+                "launch_variant": info["fast_variant"],
                 "algorithmic_bytes_per_launch": algo, "peak_source": f"{peak_kind} hbm_gbs (copy)",
                 "per_kernel_ms": {k: round(v, 4) for k, v in avg.items()},
                 "per_kernel_frac": {k: round(algo / (v / 1e3) / 1e9 / peak, 4) for k, v in avg.items()}}

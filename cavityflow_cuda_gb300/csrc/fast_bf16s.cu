@@ -1,6 +1,6 @@
 // fast_bf16s.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
-// step kernels and the batch kernels for BF16S storage (one translation unit per storage type, so
-// they compile in parallel).
+// step kernels and the batch kernels for BF16S storage (one translation unit per
+// storage type, so they compile in parallel).
 #include "lbm_fast.cuh"
 #include "lbm_kernels.h"
 #include "lbm_tma.cuh"
@@ -8,21 +8,21 @@
 namespace lbm {
 
 cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
-                           cudaStream_t st)
+                              cudaStream_t st)
 {
     return launch_fast_menu<BF16S>(variant, alpha, dd, g, p, lid_y, st);
 }
 
 cudaError_t launch_tma_bf16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
-                          int consumer_warps, int* err, cudaStream_t st)
+                             int consumer_warps, int* err, cudaStream_t st)
 {
     return launch_tma_impl<BF16S>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
 }
 
 cudaError_t launch_batch_bf16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                            long long vblocks, cudaStream_t st)
+                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
 {
-    return launch_batch_menu<BF16S>(variant, alpha, pool, doms, ndom, vblocks, st);
+    return launch_batch_menu<BF16S>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
 }
 
 }  // namespace lbm

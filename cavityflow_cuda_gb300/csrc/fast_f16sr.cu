@@ -1,0 +1,28 @@
+// fast_f16sr.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
+// step kernels and the batch kernels for F16SR storage (one translation unit per
+// storage type, so they compile in parallel).
+#include "lbm_fast.cuh"
+#include "lbm_kernels.h"
+#include "lbm_tma.cuh"
+
+namespace lbm {
+
+cudaError_t launch_fast_f16sr(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                              cudaStream_t st)
+{
+    return launch_fast_menu<F16SR>(variant, alpha, dd, g, p, lid_y, st);
+}
+
+cudaError_t launch_tma_f16sr(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
+                             int consumer_warps, int* err, cudaStream_t st)
+{
+    return launch_tma_impl<F16SR>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
+}
+
+cudaError_t launch_batch_f16sr(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+{
+    return launch_batch_menu<F16SR>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+}
+
+}  // namespace lbm

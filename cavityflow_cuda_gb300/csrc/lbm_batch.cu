@@ -39,6 +39,7 @@ struct lbm_batch {
     std::vector<lbm_solver*> views;
     std::vector<lbm::BatchDomain> table;
     lbm::BatchDomain* dtable = nullptr;
+    uint32_t* step_words = nullptr;  // [0] first step of a graph replay, [1] zero
     long long vblocks[2] = {0, 0};  // virtual blocks of the alpha and the beta kernel
     long long interior_cells = 0;
     cudaStream_t capture_stream = nullptr;
@@ -68,6 +69,7 @@ int build_table(lbm_batch* b)
             lbm::fast_variant_shape(b->storage, b->variant, kind == 0, d.g.nx, cpt, block);
             const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
             d.block_start[kind] = next;
+            d.step0 = 0;  // every domain is at the batch's step
             next += (groups + block - 1) / block;
         }
         b->vblocks[kind] = next;
@@ -78,10 +80,13 @@ int build_table(lbm_batch* b)
     return LBM_OK;
 }
 
-cudaError_t batch_launch(lbm_batch* b, int variant, bool alpha, cudaStream_t st)
+// One step of every domain.  Its stochastic-rounding step is step_off, or
+// word 0 + step_off inside a graph (in_graph).
+cudaError_t batch_launch(lbm_batch* b, int variant, bool alpha, cudaStream_t st, uint32_t step_off,
+                         bool in_graph = false)
 {
     return lbm::launch_batch_step(b->storage, variant, alpha, b->pool, b->dtable, (int)b->views.size(),
-                                  b->vblocks[alpha ? 0 : 1], st);
+                                  b->vblocks[alpha ? 0 : 1], b->step_words + (in_graph ? 0 : 1), step_off, st);
 }
 
 void sync_views(lbm_batch* b)
@@ -104,6 +109,7 @@ void free_batch(lbm_batch* b)
     }
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->dtable) cudaFree(b->dtable);
+    if (b->step_words) cudaFree(b->step_words);
     if (b->pool) cudaFree(b->pool);
     delete b;
 }
@@ -116,7 +122,7 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
 {
     if (!domains || !out || count <= 0) return fail(LBM_ERR_INVALID_ARGUMENT, "domains, count and out are required");
     *out = nullptr;
-    if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_BF16S)
+    if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
     for (int i = 0; i < count; ++i)
         for (int d = 0; d < 3; ++d)
@@ -159,6 +165,9 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc batch table"));
     e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) return bail(cuda_fail(e, "cudaStreamCreate"));
+    e = cudaMalloc(&b->step_words, 2 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(b->step_words, 0, 2 * sizeof(uint32_t));
+    if (e != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc batch step words"));
 
     b->views.reserve((size_t)count);
     for (int i = 0; i < count; ++i) {
@@ -229,7 +238,7 @@ int lbm_batch_run(lbm_batch* b, int64_t steps, void* stream)
     CK(cudaSetDevice(b->device), "cudaSetDevice");
     int64_t left = steps;
     auto one = [&](bool alpha) -> int {
-        CK(batch_launch(b, b->variant, alpha, st), alpha ? "batch alpha launch" : "batch beta launch");
+        CK(batch_launch(b, b->variant, alpha, st, (uint32_t)b->counter), alpha ? "batch alpha launch" : "batch beta launch");
         b->counter += 1;
         b->last_alpha = alpha;
         return LBM_OK;
@@ -247,8 +256,8 @@ int lbm_batch_run(lbm_batch* b, int64_t steps, void* stream)
             CK(cudaStreamBeginCapture(b->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             cudaError_t e = cudaSuccess;
             for (int i = 0; i < kBatchGraphPairs && e == cudaSuccess; ++i) {
-                e = batch_launch(b, b->variant, true, b->capture_stream);
-                if (e == cudaSuccess) e = batch_launch(b, b->variant, false, b->capture_stream);
+                e = batch_launch(b, b->variant, true, b->capture_stream, (uint32_t)(2 * i), true);
+                if (e == cudaSuccess) e = batch_launch(b, b->variant, false, b->capture_stream, (uint32_t)(2 * i + 1), true);
             }
             cudaError_t e2 = cudaStreamEndCapture(b->capture_stream, &graph);
             lbm::add_launches(before - lbm::kernel_launches());
@@ -262,6 +271,8 @@ int lbm_batch_run(lbm_batch* b, int64_t steps, void* stream)
             }
         }
         while (left >= per_graph) {
+            if (lbm::storage_stochastic(b->storage))
+                CK(lbm::launch_set_step(b->step_words, (uint32_t)b->counter, st), "step word launch");
             CK(cudaGraphLaunch(b->graph, st), "cudaGraphLaunch");
             lbm::add_launches(per_graph);
             b->counter += per_graph;
@@ -305,15 +316,15 @@ int lbm_batch_autotune(lbm_batch* b, int32_t pairs, int32_t* best, float* ms_per
     cudaError_t e = cudaMemcpyAsync(saved, b->pool, b->pool_bytes, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
-    if (e == cudaSuccess && b->last_alpha) e = batch_launch(b, b->variant, false, st);
+    if (e == cudaSuccess && b->last_alpha) e = batch_launch(b, b->variant, false, st, 0);
     int r = LBM_OK;
     for (int v = 0; v < lbm::kRegisterVariants && e == cudaSuccess && r == LBM_OK; ++v) {
         b->variant = v;
         if ((r = build_table(b))) break;
         for (int i = 0; i < 1 + pairs && e == cudaSuccess; ++i) {  // first pair warms up
             if (i == 1) e = cudaEventRecord(e0, st);
-            if (e == cudaSuccess) e = batch_launch(b, v, true, st);
-            if (e == cudaSuccess) e = batch_launch(b, v, false, st);
+            if (e == cudaSuccess) e = batch_launch(b, v, true, st, 0);
+            if (e == cudaSuccess) e = batch_launch(b, v, false, st, 0);
         }
         if (e == cudaSuccess) e = cudaEventRecord(e1, st);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);

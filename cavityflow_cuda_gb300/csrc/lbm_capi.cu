@@ -91,6 +91,7 @@ int lbm_detail::default_variant(int storage)
     case LBM_STORAGE_F32: return 8;
     case LBM_STORAGE_F16S: return 10;
     case LBM_STORAGE_BF16S: return 11;
+    case LBM_STORAGE_F16SR: return 10;
     default: return 3;
     }
 }
@@ -105,6 +106,7 @@ namespace {
 
 
 int* lbm_detail::err_flag(lbm_solver* s) { return reinterpret_cast<int*>(s->counts + 2); }
+uint32_t* lbm_detail::step_words(lbm_solver* s) { return reinterpret_cast<uint32_t*>(s->counts + 4); }
 
 // Reads and clears the kernels' timeout flag after the device is idle.
 int lbm_detail::check_kernel_flag(lbm_solver* s)
@@ -178,8 +180,11 @@ int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, 
 {
     int3 o, n;
     cudaError_t e;
+    lbm::Params p = s->p;  // this step's stochastic-rounding key
+    p.step_base = step_words(s) + 1;
+    p.step_off = (uint32_t)s->counter;
     if (!origin && s->lid_y >= 0) {
-        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, p, s->lid_y, err_flag(s), st);
     } else {
         if (origin) {
             int r = resolve_cuboid(s, origin, size, o, n);
@@ -188,7 +193,7 @@ int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, 
             o = make_int3(0, 0, 0);
             n = make_int3(s->g.nx + 2, s->g.ny + 2, s->g.nz + 2);
         }
-        e = lbm::launch_general_step(s->storage, alpha, s->dd, s->flags, s->g, s->p, o, n, st);
+        e = lbm::launch_general_step(s->storage, alpha, s->dd, s->flags, s->g, p, o, n, st);
     }
     if (e != cudaSuccess) return cuda_fail(e, alpha ? "alpha step launch" : "beta step launch");
     s->counter += 1;
@@ -375,7 +380,7 @@ extern "C" {
 int lbm_derive_lattice(const lbm_physical* phys, int32_t storage, lbm_lattice* out)
 {
     if (!phys || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
-    if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_BF16S)
+    if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
     for (int d = 0; d < 3; ++d)
         if (phys->domain_size[d] <= 0 || !(phys->domain_length[d] > 0))
@@ -399,7 +404,7 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
     for (int d = 0; d < 3; ++d)
         if (prm->size[d] <= 0 || prm->size[d] > (1 << 20))
             return fail(LBM_ERR_INVALID_ARGUMENT, "domain size must be in [1, 2^20]");
-    if (prm->storage < LBM_STORAGE_F64 || prm->storage > LBM_STORAGE_BF16S)
+    if (prm->storage < LBM_STORAGE_F64 || prm->storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", prm->storage);
     for (int f = 0; f < 6; ++f)
         if (!valid_flag(prm->boundary[f])) return fail(LBM_ERR_INVALID_ARGUMENT, "invalid boundary flag %d", prm->boundary[f]);
@@ -446,10 +451,12 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
     }
     if ((e = cudaMalloc(&s->flags, flag_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc flags"));
     if ((e = cudaMalloc(&s->scratch, scratch_bytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc scratch"));
-    if ((e = cudaMalloc(&s->counts, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMalloc(&s->counts, 6 * sizeof(unsigned long long))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMalloc counters"));
-    if ((e = cudaMemset(s->counts, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    if ((e = cudaMemset(s->counts, 0, 6 * sizeof(unsigned long long))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMemset counters"));
+    s->p.step_base = step_words(s) + 1;  // direct launches: step = step_off
+    s->p.step_off = 0;
     if ((e = cudaMallocHost(&s->host_out, 4 * sizeof(double))) != cudaSuccess)
         return bail(cuda_fail(e, "cudaMallocHost"));
     if ((e = cudaStreamCreateWithFlags(&s->capture_stream, cudaStreamNonBlocking)) != cudaSuccess)
@@ -514,6 +521,8 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     lbm::fast_variant_shape(s->storage, s->variant, true, s->g.nx, info->cells_per_thread, info->block_threads);
     lbm::fast_variant_shape(s->storage, s->variant, false, s->g.nx, info->beta_cells_per_thread,
                             info->beta_block_threads);
+    info->beta_block_exchange =
+        s->variant < lbm::kRegisterVariants && lbm::kFastMenu[s->variant].block_exchange ? 1 : 0;
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
@@ -588,11 +597,16 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             const long long before = lbm::kernel_launches();
             CK(cudaStreamBeginCapture(s->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
             cudaError_t e = cudaSuccess;
+            // launch i of the graph is step (word 0) + i
+            lbm::Params p = s->p;
+            p.step_base = step_words(s);
             for (int i = 0; i < kGraphPairs && e == cudaSuccess; ++i) {
-                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, s->p, s->lid_y, err_flag(s),
+                p.step_off = (uint32_t)(2 * i);
+                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, p, s->lid_y, err_flag(s),
                                           s->capture_stream);
+                p.step_off = (uint32_t)(2 * i + 1);
                 if (e == cudaSuccess)
-                    e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y,
+                    e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, p, s->lid_y,
                                               err_flag(s), s->capture_stream);
             }
             cudaError_t e2 = cudaStreamEndCapture(s->capture_stream, &graph);
@@ -608,6 +622,8 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             }
         }
         while (left >= per_graph) {
+            if (lbm::storage_stochastic(s->storage))
+                CK(lbm::launch_set_step(step_words(s), (uint32_t)s->counter, st), "step word launch");
             CK(cudaGraphLaunch(s->graph, st), "cudaGraphLaunch");
             lbm::add_launches(per_graph);
             s->counter += per_graph;

@@ -100,43 +100,138 @@ inline Grid make_grid(int nx, int ny, int nz, int elem_bytes)
 }
 
 // ---------------------------------------------------------------------------
-// Storage types.  F64/F32 hold f_i; F16S/BF16S hold the deviation f_i - w_i
-// as raw 16-bit patterns.  `T` is the arithmetic type of the collision.
+// Storage types.  F64/F32 hold f_i; F16S/BF16S/F16SR hold the deviation
+// f_i - w_i as raw 16-bit patterns.  `T` is the arithmetic type of the
+// collision.  `stochastic` types round the step kernels' stores with a dither
+// keyed by (cell, population, time step): store_sr(v, d) with d from
+// sr_dither below; `store` (round to nearest) serves every other write.
 // ---------------------------------------------------------------------------
 struct F64 {
     using bits = double;
     using T = double;
     static constexpr bool shifted = false;
+    static constexpr bool stochastic = false;
     __device__ static T load(bits b) { return b; }
     __device__ static bits store(T v) { return v; }
+    __device__ static T load_step(bits b) { return load(b); }
+    static constexpr int kStepLog2 = 0;
 };
 struct F32 {
     using bits = float;
     using T = float;
     static constexpr bool shifted = false;
+    static constexpr bool stochastic = false;
     __device__ static T load(bits b) { return b; }
     __device__ static bits store(T v) { return v; }
+    __device__ static T load_step(bits b) { return load(b); }
+    static constexpr int kStepLog2 = 0;
 };
 struct F16S {
     using bits = unsigned short;
     using T = float;
     static constexpr bool shifted = true;
+    static constexpr bool stochastic = false;
     __device__ static T load(bits b) { return __half2float(__ushort_as_half(b)); }
     __device__ static bits store(T v) { return __half_as_ushort(__float2half_rn(v)); }
+    __device__ static T load_step(bits b) { return load(b); }
+    static constexpr int kStepLog2 = 0;
 };
 struct BF16S {
     using bits = unsigned short;
     using T = float;
     static constexpr bool shifted = true;
+    static constexpr bool stochastic = false;
     __device__ static T load(bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
     __device__ static bits store(T v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
+    __device__ static T load_step(bits b) { return load(b); }
+    static constexpr int kStepLog2 = 0;
 };
 
-// Scalar lattice parameters of one domain.
+// Stochastic-rounding keys.  sr_hash mixes a cell's index in the compact
+// (nx+2)(ny+2)(nz+2) layout with the time step (the "lowbias32" integer hash
+// of C. Wellons); sr_dither gives population k of that cell the top 13 bits
+// of a Weyl sequence started at the hash: uniform over [0, 2^13) from cell to
+// cell and step to step.
+__host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t cell, uint32_t step)
+{
+    uint32_t x = cell ^ (step * 0x9E3779B9u);
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t sr_dither(uint32_t h, int k)
+{
+    return (h * 0x2545F491u + (uint32_t)k * 0x9E3779B9u) >> 19;
+}
+
+// IEEE half deviations scaled by 2^kF16SRScale, rounded stochastically.
+// Scaling by a power of two is exact; it moves deviations down to 2^-26 out
+// of the half subnormal range, where a 13-bit dither would not cover every
+// discarded bit.  Rounding: the dither is added to the float's bit pattern
+// below the 13 bits that half precision drops (this acts on the magnitude;
+// the sign bit is above it), then the value is truncated toward zero, so a
+// value between two halves rounds away from zero with probability equal to
+// its distance from the smaller one: the expected stored value is exact.
+// Round to nearest (the rounding error's sign fixed by the value) lets slow
+// changes stall below half a unit and bias the flow; the dither removes that.
+//
+// The step kernels work in the scaled units (load_step, store_sr): the
+// collision is linear in the deviations except for |j|^2 and u^2, whose
+// constants collide_shifted<kStepLog2> divides by the scale, so every result
+// is exactly 2^12 times the unscaled one and no multiply by the scale is
+// needed per population.  load/store (getters, setters) use plain units.
+constexpr int kF16SRScale = 12;
+struct F16SR {
+    using bits = unsigned short;
+    using T = float;
+    static constexpr bool shifted = true;
+    static constexpr bool stochastic = true;
+    static constexpr int kStepLog2 = kF16SRScale;
+    __device__ static T load(bits b)
+    {
+        return __half2float(__ushort_as_half(b)) * __uint_as_float((uint32_t)(127 - kF16SRScale) << 23);
+    }
+    __device__ static bits store(T v)
+    {
+        return __half_as_ushort(__float2half_rn(v * __uint_as_float((uint32_t)(127 + kF16SRScale) << 23)));
+    }
+    __device__ static T load_step(bits b) { return __half2float(__ushort_as_half(b)); }
+    __device__ static bits store_sr(T scaled, uint32_t dither)
+    {
+        return __half_as_ushort(__float2half_rz(__uint_as_float(__float_as_uint(scaled) + dither)));
+    }
+};
+
+// The time step that keys stochastic rounding: *step_base + step_off (a graph
+// replays its launches with the word at step_base rewritten and step_off
+// fixed).  Other storage types never read it.
+template <class St>
+__device__ __forceinline__ uint32_t step_of(const uint32_t* step_base, uint32_t step_off)
+{
+    if constexpr (St::stochastic) return *step_base + step_off;
+    else return 0u;
+}
+
+// A step kernel's store of population k of a cell with hash h.
+template <class St>
+__device__ __forceinline__ typename St::bits store_pop(typename St::T v, uint32_t h, int k)
+{
+    if constexpr (St::stochastic) return St::store_sr(v, sr_dither(h, k));
+    else return St::store(v);
+}
+
+// Scalar lattice parameters of one domain, and the time step of the next
+// launch, *step_base + step_off (it keys stochastic rounding; step_base points
+// to device memory so that captured graphs can be replayed at later steps).
 struct Params {
     double inv_tau;
     double lid_u;
     double gx, gy, gz;
+    const uint32_t* step_base = nullptr;
+    uint32_t step_off = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -280,6 +375,7 @@ __device__ __forceinline__ void relax_pair_shifted(float& sp, float& sm, float w
     sm = __fmaf_rn(omega, (even - odd) - sm, sm);
 }
 
+template <int E = 0>
 __device__ __forceinline__ void collide_shifted(float* s, float omega)
 {
     const float a01 = s[0] + s[1], d01 = s[0] - s[1];
@@ -296,10 +392,12 @@ __device__ __forceinline__ void collide_shifted(float* s, float omega)
     const float jy = ((d23 + d45) - d67) + (d1213 + d1415);
     const float jz = ((d89 - d1011) + (d1213 - d1415)) + d1617;
     const float vel2 = __fmaf_rn(jz, jz, __fmaf_rn(jy, jy, jx * jx));
-    const float P = __fmaf_rn(-1.5f, vel2, drho);
+    // with deviations scaled by 2^E the quadratic terms carry 2^-E (exact)
+    constexpr float inv_scale = 1.0f / (float)(1u << E);
+    const float P = __fmaf_rn(-1.5f * inv_scale, vel2, drho);
     const float wa = 1.0f / 18.0f, wd = 1.0f / 36.0f;
     const float waP = wa * P, wdP = wd * P;
-    const float wa3 = 3.0f * wa, wa45 = 4.5f * wa, wd3 = 3.0f * wd, wd45 = 4.5f * wd;
+    const float wa3 = 3.0f * wa, wa45 = (4.5f * wa) * inv_scale, wd3 = 3.0f * wd, wd45 = (4.5f * wd) * inv_scale;
     relax_pair_shifted(s[0], s[1], wa3, wa45, waP, jx, omega);
     relax_pair_shifted(s[2], s[3], wa3, wa45, waP, jy, omega);
     relax_pair_shifted(s[4], s[5], wd3, wd45, wdP, jx + jy, omega);
@@ -317,7 +415,7 @@ __device__ __forceinline__ void collide_shifted(float* s, float omega)
 template <class St>
 __device__ __forceinline__ void collide(typename St::T* f, typename St::T inv_tau)
 {
-    if constexpr (St::shifted) collide_shifted(f, inv_tau);
+    if constexpr (St::shifted) collide_shifted<St::kStepLog2>(f, inv_tau);
     else collide_fluid(f, inv_tau);
 }
 
@@ -327,6 +425,17 @@ template <typename T>
 __device__ __forceinline__ void inject(T* f, T rho0, T lid_u)
 {
     equilibrium(rho0, lid_u, T(0), T(0), f);
+}
+
+// The same in a storage type's step units (scaled deviations for F16SR).
+template <class St>
+__device__ __forceinline__ void inject_step(typename St::T* f, typename St::T rho0, typename St::T lid_u)
+{
+    inject(f, rho0, lid_u);
+    if constexpr (St::kStepLog2 != 0) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) f[k] *= (float)(1u << St::kStepLog2);
+    }
 }
 
 }  // namespace lbm

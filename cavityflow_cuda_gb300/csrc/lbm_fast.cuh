@@ -111,7 +111,7 @@ __device__ __forceinline__ B shfl_down_bits(B v, int d)
 template <class St, int CPT>
 __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                             const typename St::T inv_tau, const typename St::T lid_u,
-                                            const int lid_y, const long long t)
+                                            const int lid_y, const long long t, const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -137,11 +137,13 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
         if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
         T c[Q];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) c[k] = St::load(f[k][v]);
-        if (lid) inject(c, rho0, lid_u);
+        for (int k = 0; k < Q; ++k) c[k] = St::load_step(f[k][v]);
+        if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
+        uint32_t h = 0;
+        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) f[opp(k)][v] = St::store(c[k]);  // population k -> slot opp(k)
+        for (int k = 0; k < Q; ++k) f[opp(k)][v] = store_pop<St>(c[k], h, k);  // population k -> slot opp(k)
     }
 #pragma unroll
     for (int k = 0; k < Q; ++k) IO::store_raw(dd + k * g.S + base, f[k]);
@@ -150,9 +152,12 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                           const typename St::T inv_tau,
-                                                          const typename St::T lid_u, const int lid_y)
+                                                          const typename St::T lid_u, const int lid_y,
+                                                          const uint32_t* __restrict__ step_base,
+                                                          const uint32_t step_off)
 {
-    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
+    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
+                         step_of<St>(step_base, step_off));
 }
 
 // Beta step of the CPT cells owned by thread index t of one domain.  All 32
@@ -162,7 +167,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
 template <class St, int CPT>
 __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                            const typename St::T inv_tau, const typename St::T lid_u,
-                                           const int lid_y, const long long t)
+                                           const int lid_y, const long long t, const uint32_t step)
 {
     using T = typename St::T;
     using IO = Vio<St, CPT>;
@@ -226,11 +231,13 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
         if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
         T c[Q];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load(p[k][v]);
-        if (lid) inject(c, rho0, lid_u);
+        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load_step(p[k][v]);
+        if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
+        uint32_t h = 0;
+        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) p[k][v] = St::store(c[k]);  // population k -> slot k at x + c_k
+        for (int k = 0; k < Q; ++k) p[k][v] = store_pop<St>(c[k], h, k);  // population k -> slot k at x + c_k
     }
 
     static_for<0, Q>([&](auto kc) {
@@ -284,7 +291,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
 template <class St, int CPT, int BLOCK>
 __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ dd, const Grid& g,
                                                const typename St::T inv_tau, const typename St::T lid_u,
-                                               const int lid_y, const long long t)
+                                               const int lid_y, const long long t, const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -371,11 +378,13 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
         if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
         T c[Q];
 #pragma unroll
-        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load(p[k][v]);
-        if (lid) inject(c, rho0, lid_u);
+        for (int k = 0; k < Q; ++k) c[opp(k)] = St::load_step(p[k][v]);
+        if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
+        uint32_t h = 0;
+        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
 #pragma unroll
-        for (int k = 0; k < Q; ++k) p[k][v] = St::store(c[k]);  // population k -> slot k at x + c_k
+        for (int k = 0; k < Q; ++k) p[k][v] = store_pop<St>(c[k], h, k);  // population k -> slot k at x + c_k
     }
 
     static_for<0, 12>([&](auto kc) {
@@ -435,17 +444,23 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_blk(typename St::bits* __restrict__ dd, const Grid g,
                                                              const typename St::T inv_tau,
-                                                             const typename St::T lid_u, const int lid_y)
+                                                             const typename St::T lid_u, const int lid_y,
+                                                          const uint32_t* __restrict__ step_base,
+                                                          const uint32_t step_off)
 {
-    beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
+    beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
+                                   step_of<St>(step_base, step_off));
 }
 
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                          const typename St::T inv_tau,
-                                                         const typename St::T lid_u, const int lid_y)
+                                                         const typename St::T lid_u, const int lid_y,
+                                                          const uint32_t* __restrict__ step_base,
+                                                          const uint32_t step_off)
 {
-    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x);
+    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
+                        step_of<St>(step_base, step_off));
 }
 
 // Cells per thread of a kernel shape for storage St (at least one).
@@ -467,16 +482,19 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
         constexpr int CPT = shape_cpt<St>(k);
         const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
         const int blocks = (int)((threads + k.block - 1) / k.block);
-        alpha_fast<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+        alpha_fast<St, CPT, k.block, k.minb>
+            <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
     } else {
         constexpr KernelShape k = fv.beta;
         constexpr int CPT = shape_cpt<St>(k);
         const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
         const int blocks = (int)((threads + k.block - 1) / k.block);
         if constexpr (fv.block_exchange)
-            beta_fast_blk<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+            beta_fast_blk<St, CPT, k.block, k.minb>
+                <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
         else
-            beta_fast<St, CPT, k.block, k.minb><<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y);
+            beta_fast<St, CPT, k.block, k.minb>
+                <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
     }
     return cudaGetLastError();
 }
@@ -519,13 +537,17 @@ struct BatchDomain {
     double lid_u;
     int lid_y;
     long long block_start[2];  // first virtual block of this domain: [0] alpha, [1] beta kernel
+    uint32_t step0;            // added to the launch's step: this domain's own step count
 };
 
 template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, bool kExchange>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
                                                           const BatchDomain* __restrict__ doms, const int ndom,
-                                                          const long long vblocks)
+                                                          const long long vblocks,
+                                                          const uint32_t* __restrict__ step_base,
+                                                          const uint32_t step_off)
 {
+    const uint32_t step = step_of<St>(step_base, step_off);
     using T = typename St::T;
     constexpr int which = kAlpha ? 0 : 1;
     // Every thread of a CTA walks the same virtual blocks, so the block-wide
@@ -539,15 +561,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         }
         const BatchDomain d = doms[lo];
         const long long t = (vb - d.block_start[which]) * BLOCK + threadIdx.x;
-        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
+        const uint32_t ds = step + d.step0;
+        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
         else if constexpr (kExchange)
-            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
-        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t);
+            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
+        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
     }
 }
 
 template <class St, int VARIANT, bool kAlpha>
-cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, long long vblocks, cudaStream_t st)
+cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, long long vblocks,
+                                const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
 {
     constexpr FastVariant fv = kFastMenu[VARIANT];
     constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
@@ -561,34 +585,38 @@ cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, l
     long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms;
     if (grid > vblocks) grid = vblocks;
     if (grid < 1) return cudaSuccess;
-    kern<<<(int)grid, k.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks);
+    kern<<<(int)grid, k.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks, step_base,
+                                        step_off);
     return cudaGetLastError();
 }
 
 template <class St, int VARIANT>
 cudaError_t launch_batch_variant(bool alpha, void* pool, const BatchDomain* doms, int ndom, long long vblocks,
-                                 cudaStream_t st)
+                                 const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
 {
-    return alpha ? launch_batch_kernel<St, VARIANT, true>(pool, doms, ndom, vblocks, st)
-                 : launch_batch_kernel<St, VARIANT, false>(pool, doms, ndom, vblocks, st);
+    return alpha ? launch_batch_kernel<St, VARIANT, true>(pool, doms, ndom, vblocks, step_base, step_off, st)
+                 : launch_batch_kernel<St, VARIANT, false>(pool, doms, ndom, vblocks, step_base, step_off, st);
 }
 
 template <class St, size_t... I>
 cudaError_t launch_batch_table(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, cudaStream_t st, std::index_sequence<I...>)
+                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st,
+                               std::index_sequence<I...>)
 {
-    using Fn = cudaError_t (*)(bool, void*, const BatchDomain*, int, long long, cudaStream_t);
+    using Fn = cudaError_t (*)(bool, void*, const BatchDomain*, int, long long, const uint32_t*, uint32_t,
+                               cudaStream_t);
     static constexpr Fn table[] = {&launch_batch_variant<St, (int)I>...};
-    return table[variant](alpha, pool, doms, ndom, vblocks, st);
+    return table[variant](alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
 }
 
 // `vblocks`: the virtual blocks of the kernel launched (alpha or beta shape).
+// The step of domain d is *step_base + step_off + d.step0.
 template <class St>
 cudaError_t launch_batch_menu(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, cudaStream_t st)
+                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
 {
     if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
-    return launch_batch_table<St>(variant, alpha, pool, doms, ndom, vblocks, st,
+    return launch_batch_table<St>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st,
                                   std::make_index_sequence<kRegisterVariants>{});
 }
 

@@ -21,7 +21,8 @@ struct lbm_solver {
     void* macros = nullptr;         // 4 * cells values (rho, jx, jy, jz)
     bool macros_fresh = false;
     double* scratch = nullptr;      // reduction partials (4 per block) + result (4)
-    unsigned long long* counts = nullptr;  // cavity-flag check counters [0..1], kernel error flag [2]
+    unsigned long long* counts = nullptr;  // cavity-flag check counters [0..1], kernel error flag [2],
+                                           // step words [4] (see step_words)
     double* host_out = nullptr;     // pinned, 4 doubles
     float* staging = nullptr;       // 16-bit storage: one packed slot cuboid
     size_t staging_elems = 0;
@@ -48,6 +49,9 @@ int default_variant(int storage);
 int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out);
 void destroy_solver(lbm_solver* s);
 int* err_flag(lbm_solver* s);
+// Two device words of the solver: [0] the first step of a graph replay,
+// [1] always zero (the base of directly launched steps).
+uint32_t* step_words(lbm_solver* s);
 int check_kernel_flag(lbm_solver* s);
 
 }  // namespace lbm_detail

@@ -141,7 +141,7 @@ static int read_header(FILE* f, const char* path, CkptHeader& h)
     if (std::fread(&h, sizeof(h), 1, f) != 1) return fail(LBM_ERR_IO, "\"%s\": truncated header", path);
     if (std::memcmp(h.magic, kMagic, 16) != 0 || h.version != 1)
         return fail(LBM_ERR_IO, "\"%s\" is not a version-1 checkpoint of this solver", path);
-    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_BF16S || h.nx <= 0 || h.ny <= 0 || h.nz <= 0)
+    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_F16SR || h.nx <= 0 || h.ny <= 0 || h.nz <= 0)
         return fail(LBM_ERR_IO, "\"%s\": corrupt header", path);
     const uint64_t cells = (uint64_t)(h.nx + 2) * (h.ny + 2) * (h.nz + 2);
     if (h.flag_bytes != cells || h.pop_bytes != (uint64_t)lbm::Q * cells * (uint64_t)elem_bytes(h.storage))

@@ -50,15 +50,17 @@ __global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t*
     T f[Q];
     if (fl == kFluid) {
 #pragma unroll
-        for (int k = 0; k < Q; ++k) f[k] = St::load(dd[k * g.S + c0]);
+        for (int k = 0; k < Q; ++k) f[k] = St::load_step(dd[k * g.S + c0]);
         if (kGravity) collide_fluid_gravity(f, inv_tau, T(prm.gx), T(prm.gy), T(prm.gz));
         else collide<St>(f, inv_tau);
     } else {
-        inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
+        inject_step<St>(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
         if (kGravity) alpha_gravity(f, T(1), T(prm.gx), T(prm.gy), T(prm.gz));
     }
+    uint32_t h = 0;
+    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y, z), step_of<St>(prm.step_base, prm.step_off));
 #pragma unroll
-    for (int k = 0; k < Q; ++k) dd[opp(k) * g.S + c0] = St::store(f[k]);
+    for (int k = 0; k < Q; ++k) dd[opp(k) * g.S + c0] = store_pop<St>(f[k], h, k);
 }
 
 template <class St>
@@ -82,12 +84,15 @@ __global__ void beta_general(typename St::bits* __restrict__ dd, const uint8_t* 
                                      : wrapped_position(g, x, y, z, k));
     T f[Q];
 #pragma unroll
-    for (int k = 0; k < Q; ++k) f[opp(k)] = St::load(dd[pos[k]]);
+    for (int k = 0; k < Q; ++k) f[opp(k)] = St::load_step(dd[pos[k]]);
     if (fl == kFluid) collide<St>(f, T(prm.inv_tau));
-    else if (fl == kInjection) inject(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
-    // GHOST_LAYER (and any other value): streamed through unchanged
+    else if (fl == kInjection) inject_step<St>(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
+    // GHOST_LAYER (and any other value): streamed through unchanged (a value
+    // read from storage is stored back exactly, also by stochastic rounding)
+    uint32_t h = 0;
+    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y, z), step_of<St>(prm.step_base, prm.step_off));
 #pragma unroll
-    for (int k = 0; k < Q; ++k) dd[pos[k]] = St::store(f[k]);
+    for (int k = 0; k < Q; ++k) dd[pos[k]] = store_pop<St>(f[k], h, k);
 }
 
 // ===========================================================================
@@ -336,6 +341,7 @@ cudaError_t with_storage(int storage, F&& f)
     case 1: return f(F32{});
     case 2: return f(F16S{});
     case 3: return f(BF16S{});
+    case 4: return f(F16SR{});
     default: return cudaErrorInvalidValue;
     }
 }
@@ -359,6 +365,15 @@ cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, co
     if (e != cudaSuccess) return e;
     init_flags<<<grid_for(g.cells(), 256, 4096), 256, 0, st>>>(flags, g, bc);
     count_launch(2);
+    return cudaGetLastError();
+}
+
+__global__ void set_step_word(uint32_t* word, uint32_t value) { *word = value; }
+
+cudaError_t launch_set_step(uint32_t* word, uint32_t value, cudaStream_t st)
+{
+    set_step_word<<<1, 1, 0, st>>>(word, value);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -399,15 +414,16 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, 
 }
 
 cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, cudaStream_t st)
+                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
 {
     if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
     count_launch();
     switch (storage) {
-    case 0: return launch_batch_f64(variant, alpha, pool, doms, ndom, vblocks, st);
-    case 1: return launch_batch_f32(variant, alpha, pool, doms, ndom, vblocks, st);
-    case 2: return launch_batch_f16s(variant, alpha, pool, doms, ndom, vblocks, st);
-    case 3: return launch_batch_bf16s(variant, alpha, pool, doms, ndom, vblocks, st);
+    case 0: return launch_batch_f64(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    case 1: return launch_batch_f32(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    case 2: return launch_batch_f16s(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    case 3: return launch_batch_bf16s(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    case 4: return launch_batch_f16sr(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -423,6 +439,7 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
         case 1: e = launch_tma_f32(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 2: e = launch_tma_f16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 3: e = launch_tma_bf16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 4: e = launch_tma_f16sr(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         default: return cudaErrorInvalidValue;
         }
         if (e == cudaSuccess) count_launch();
@@ -434,6 +451,7 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
     case 1: return launch_fast_f32(variant, alpha, dd, g, p, lid_y, st);
     case 2: return launch_fast_f16s(variant, alpha, dd, g, p, lid_y, st);
     case 3: return launch_fast_bf16s(variant, alpha, dd, g, p, lid_y, st);
+    case 4: return launch_fast_f16sr(variant, alpha, dd, g, p, lid_y, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -26,6 +26,11 @@ void add_launches(long long n);
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
 cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
+// Storage types whose step kernels round stochastically, keyed by the step
+// (Params::step_base/step_off); a graph replaying such launches needs the
+// word at step_base set to its first step before each replay.
+inline bool storage_stochastic(int storage) { return storage == 4; }
+cudaError_t launch_set_step(uint32_t* word, uint32_t value, cudaStream_t st);
 // Box-cavity step.  Variants 0..kRegisterVariants-1 index kFastMenu, the
 // register kernels of lbm_fast.cuh; the rest index kTmaMenu, the
 // row-pipelined bulk-copy kernels of lbm_tma.cuh.  A variant that does not
@@ -87,15 +92,17 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cells
 // Batches of box cavities (lbm_fast.cuh): register variants only.
 struct BatchDomain;
 cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, cudaStream_t st);
+                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
 cudaError_t launch_batch_f64(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                             long long vblocks, cudaStream_t st);
+                             long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
 cudaError_t launch_batch_f32(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                             long long vblocks, cudaStream_t st);
+                             long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
 cudaError_t launch_batch_f16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, cudaStream_t st);
+                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
+cudaError_t launch_batch_f16sr(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
+                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
 cudaError_t launch_batch_bf16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, cudaStream_t st);
+                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
@@ -104,6 +111,8 @@ cudaError_t launch_fast_f16s(int variant, bool alpha, void* dd, const Grid& g, c
                              cudaStream_t st);
 cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                               cudaStream_t st);
+cudaError_t launch_fast_f16sr(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                              cudaStream_t st);
 cudaError_t launch_tma_f64(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
                            int consumer_warps, int* err, cudaStream_t st);
 cudaError_t launch_tma_f32(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
@@ -111,6 +120,8 @@ cudaError_t launch_tma_f32(bool alpha, void* dd, const Grid& g, const Params& p,
 cudaError_t launch_tma_f16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
                             int consumer_warps, int* err, cudaStream_t st);
 cudaError_t launch_tma_bf16s(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows,
+                             int stages, int consumer_warps, int* err, cudaStream_t st);
+cudaError_t launch_tma_f16sr(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows,
                              int stages, int consumer_warps, int* err, cudaStream_t st);
 cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t* flags, const Grid& g,
                                 const Params& p, int3 origin, int3 size, cudaStream_t st);

@@ -122,6 +122,7 @@ struct lbm_server {
     std::vector<lbm::BatchDomain> table;
     lbm::BatchDomain* dtable = nullptr;
     size_t dtable_cap = 0;
+    uint32_t* zero_word = nullptr;  // step base of the round launches (a request's step is its own count)
     cudaStream_t stream = nullptr;
     int64_t next_id = 1;
     int64_t completed = 0;
@@ -226,6 +227,7 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&v
         d.inv_tau = v->p.inv_tau;
         d.lid_u = v->p.lid_u;
         d.lid_y = v->g.ny;
+        d.step0 = (uint32_t)(reqs[i]->spec.steps - reqs[i]->remaining);  // steps this request has taken
         for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
             int cpt = 1, block = 1;
             lbm::fast_variant_shape(s->cfg.storage, s->variant, kind == 0, d.g.nx, cpt, block);
@@ -279,7 +281,7 @@ int lbm_server_create(const lbm_server_config* cfg, lbm_server** out)
 {
     if (!cfg || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
-    if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_BF16S)
+    if (cfg->storage < LBM_STORAGE_F64 || cfg->storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", cfg->storage);
     if (cfg->budget_bytes < (int64_t)(1 << 20)) return fail(LBM_ERR_INVALID_ARGUMENT, "budget below 1 MiB");
     if (cfg->max_round_steps < 2) return fail(LBM_ERR_INVALID_ARGUMENT, "max_round_steps must be >= 2");
@@ -303,6 +305,8 @@ int lbm_server_create(const lbm_server_config* cfg, lbm_server** out)
     }
     cudaError_t e = cudaMalloc((void**)&s->arena, s->arena_bytes);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&s->zero_word, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(s->zero_word, 0, sizeof(uint32_t));
     if (e != cudaSuccess) {
         lbm_server_destroy(s);
         return cuda_fail(e, "server allocation");
@@ -325,6 +329,7 @@ int lbm_server_destroy(lbm_server* s)
     for (Request* r : s->queue) delete r;
     for (auto& kv : s->finished) delete kv.second;
     if (s->dtable) cudaFree(s->dtable);
+    if (s->zero_word) cudaFree(s->zero_word);
     if (s->arena) cudaFree(s->arena);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
@@ -400,7 +405,7 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     const auto t_start = std::chrono::steady_clock::now();
     for (int64_t i = 0; i < q; ++i)
         CK(lbm::launch_batch_step(s->cfg.storage, s->variant, (i & 1) == 0, s->arena, s->dtable, (int)run.size(),
-                                  vblocks[i & 1], s->stream),
+                                  vblocks[i & 1], s->zero_word, (uint32_t)i, s->stream),
            "server step launch");
     CK(cudaStreamSynchronize(s->stream), "server round");
     const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();

@@ -144,10 +144,13 @@ template <class St, bool kAlpha>
 __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __restrict__ dd, const Grid g,
                                                            const typename St::T inv_tau,
                                                            const typename St::T lid_u, const int lid_y,
-                                                           const int R, const int stages, int* __restrict__ err)
+                                                           const int R, const int stages, int* __restrict__ err,
+                                                           const uint32_t* __restrict__ step_base,
+                                                           const uint32_t step_off)
 {
     using T = typename St::T;
     using bits = typename St::bits;
+    const uint32_t step = step_of<St>(step_base, step_off);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const unsigned slot_elems = (unsigned)(R * g.P);          // one slot of a buffer
     const unsigned stage_elems = (unsigned)Q * slot_elems;    // one buffer
@@ -252,7 +255,6 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
         tma::mbar_test(&full[s], parity);  // phase already complete: this lane's acquire of the data
         int z, y0, rn;
         unit_rows(i, z, y0, rn);
-        (void)z;
         bits* sb = buf + (size_t)s * stage_elems;
         for (int r = 0; r < rn; ++r) {
             const bool lid = (y0 + r == lid_y);
@@ -261,18 +263,22 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
                 T f[Q];
                 if constexpr (kAlpha) {
 #pragma unroll
-                    for (int k = 0; k < Q; ++k) f[k] = St::load(sb[k * slot_elems + col]);
-                    if (lid) inject(f, rho0, lid_u);
+                    for (int k = 0; k < Q; ++k) f[k] = St::load_step(sb[k * slot_elems + col]);
+                    if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
+                    uint32_t h = 0;
+                    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y0 + r, z), step);
 #pragma unroll
-                    for (int k = 0; k < Q; ++k) sb[opp(k) * slot_elems + col] = St::store(f[k]);
+                    for (int k = 0; k < Q; ++k) sb[opp(k) * slot_elems + col] = store_pop<St>(f[k], h, k);
                 } else {
 #pragma unroll
-                    for (int k = 0; k < Q; ++k) f[opp(k)] = St::load(sb[k * slot_elems + col + dir_x(k)]);
-                    if (lid) inject(f, rho0, lid_u);
+                    for (int k = 0; k < Q; ++k) f[opp(k)] = St::load_step(sb[k * slot_elems + col + dir_x(k)]);
+                    if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
+                    uint32_t h = 0;
+                    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y0 + r, z), step);
 #pragma unroll
-                    for (int k = 0; k < Q; ++k) sb[k * slot_elems + col + dir_x(k)] = St::store(f[k]);
+                    for (int k = 0; k < Q; ++k) sb[k * slot_elems + col + dir_x(k)] = store_pop<St>(f[k], h, k);
                 }
             }
         }
@@ -320,7 +326,7 @@ cudaError_t launch_tma_impl(bool alpha, void* dd, const Grid& g, const Params& p
     const long long units = (long long)((g.ny + R - 1) / R) * g.nz;
     const long long grid = units < (long long)per_sm * sms ? units : (long long)per_sm * sms;
     kern<<<(int)grid, threads, smem, st>>>(static_cast<bits*>(dd), g, T(p.inv_tau), T(p.lid_u), lid_y, R, stages,
-                                          err);
+                                          err, p.step_base, p.step_off);
     return cudaGetLastError();
 }
 

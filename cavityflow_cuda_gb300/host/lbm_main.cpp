@@ -3,7 +3,7 @@
 // src/CManager.cpp:27-105 for one subdomain, CController::run
 // src/CController.cpp:1354-1510) on the C ABI of liblbm_gb300.so.
 //
-//   lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s] [--device N]
+//   lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--device N]
 //             [--fast-variant V | --autotune] [--vtk-binary]
 //             [--checkpoint FILE --checkpoint-every N] [--resume FILE]
 //
@@ -68,7 +68,7 @@ struct Options {
 
 void usage()
 {
-    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s] [--device N]\n"
+    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--device N]\n"
                  "                 [--fast-variant V | --autotune] [--vtk-binary]\n"
                  "                 [--checkpoint FILE --checkpoint-every N] [--resume FILE]\n";
 }
@@ -91,6 +91,7 @@ Options parse(int argc, char** argv)
             else if (v == "f32") o.storage = LBM_STORAGE_F32;
             else if (v == "f16s") o.storage = LBM_STORAGE_F16S;
             else if (v == "bf16s") o.storage = LBM_STORAGE_BF16S;
+            else if (v == "f16sr") o.storage = LBM_STORAGE_F16SR;
             else die("unknown storage " + v);
         } else if (a == "--device") {
             o.device = std::atoi(value().c_str());

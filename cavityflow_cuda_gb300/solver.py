@@ -24,7 +24,7 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "lbm_gb300.h")
 
 OBSTACLE, FLUID, VELOCITY_INJECTION, GHOST_LAYER = 1, 2, 4, 8
 DIRECTION_ALL, LEFT, RIGHT, BOTTOM, TOP, BACK, FRONT = -1, 0, 1, 2, 3, 4, 5
-STORAGE = {"f64": 0, "f32": 1, "f16s": 2, "bf16s": 3}
+STORAGE = {"f64": 0, "f32": 1, "f16s": 2, "bf16s": 3, "f16sr": 4}
 
 _lib: Optional[C.CDLL] = None
 
@@ -71,7 +71,8 @@ class _Info(C.Structure):
                 ("vector_cells", C.c_int32), ("step_counter", C.c_int64), ("last_step_was_alpha", C.c_int32),
                 ("fast_path", C.c_int32), ("fast_variant", C.c_int32), ("cells_per_thread", C.c_int32),
                 ("block_threads", C.c_int32), ("beta_cells_per_thread", C.c_int32),
-                ("beta_block_threads", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
+                ("beta_block_threads", C.c_int32), ("beta_block_exchange", C.c_int32), ("reserved", C.c_int32),
+                ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
                 ("device_bytes", C.c_int64)]
 
 

@@ -65,13 +65,20 @@ enum { LBM_DIRECTION_ALL = -1, LBM_LEFT = 0, LBM_RIGHT = 1, LBM_BOTTOM = 2, LBM_
        LBM_BACK = 4, LBM_FRONT = 5 };
 
 /* Storage precision of the population array.  F64 and F32 reproduce the
- * reference kernels' arithmetic exactly.  F16S and BF16S store the
- * deviation f_i - w_i in 16 bits and collide in FP32 registers. */
+ * reference kernels' arithmetic exactly.  F16S, BF16S and F16SR store the
+ * deviation f_i - w_i in 16 bits and collide in FP32 registers; F16S and
+ * BF16S round to nearest, F16SR keeps IEEE half values of the deviation
+ * times 2^12 and rounds the time steps' stores stochastically, with a dither
+ * keyed by (cell, population, step), so that results are reproducible.
+ * Rounding to nearest biases slowly changing populations; stochastic
+ * rounding does not, and is several times more accurate against an FP64 run
+ * at the same 2 bytes per value. */
 typedef enum lbm_storage {
     LBM_STORAGE_F64 = 0,
     LBM_STORAGE_F32 = 1,
     LBM_STORAGE_F16S = 2,
-    LBM_STORAGE_BF16S = 3
+    LBM_STORAGE_BF16S = 3,
+    LBM_STORAGE_F16SR = 4
 } lbm_storage;
 
 /* ---- parameters ----------------------------------------------------------- */
@@ -184,6 +191,9 @@ typedef struct lbm_info {
     int32_t block_threads;      /* threads per block of its alpha kernel       */
     int32_t beta_cells_per_thread;  /* the same for its beta kernel            */
     int32_t beta_block_threads;
+    int32_t beta_block_exchange;    /* 1: beta exchanges edge elements across
+                                       the block (beta_fast_blk)               */
+    int32_t reserved;
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */

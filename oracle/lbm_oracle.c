@@ -132,8 +132,12 @@ static void relax_pair_shifted(float* sp, float* sm, float w3, float w45, float 
     *sm = fmaf(omega, (even - odd) - *sm, *sm);
 }
 
-static void collide_shifted(float* s, float omega)
+/* e: the deviations are scaled by 2^e (kind 2 collides in those units); the
+ * quadratic terms' constants carry 2^-e, so every result is exactly 2^e times
+ * the unscaled one. */
+static void collide_shifted(float* s, float omega, int e)
 {
+    const float inv_scale = 1.0f / (float)(1u << e);
     const float a01 = s[0] + s[1], d01 = s[0] - s[1];
     const float a23 = s[2] + s[3], d23 = s[2] - s[3];
     const float a45 = s[4] + s[5], d45 = s[4] - s[5];
@@ -148,10 +152,10 @@ static void collide_shifted(float* s, float omega)
     const float jy = ((d23 + d45) - d67) + (d1213 + d1415);
     const float jz = ((d89 - d1011) + (d1213 - d1415)) + d1617;
     const float vel2 = fmaf(jz, jz, fmaf(jy, jy, jx * jx));
-    const float P = fmaf(-1.5f, vel2, drho);
+    const float P = fmaf(-1.5f * inv_scale, vel2, drho);
     const float wa = 1.0f / 18.0f, wd = 1.0f / 36.0f;
     const float waP = wa * P, wdP = wd * P;
-    const float wa3 = 3.0f * wa, wa45 = 4.5f * wa, wd3 = 3.0f * wd, wd45 = 4.5f * wd;
+    const float wa3 = 3.0f * wa, wa45 = (4.5f * wa) * inv_scale, wd3 = 3.0f * wd, wd45 = (4.5f * wd) * inv_scale;
     relax_pair_shifted(&s[0], &s[1], wa3, wa45, waP, jx, omega);
     relax_pair_shifted(&s[2], &s[3], wa3, wa45, waP, jy, omega);
     relax_pair_shifted(&s[4], &s[5], wd3, wd45, wdP, jx + jy, omega);
@@ -164,8 +168,68 @@ static void collide_shifted(float* s, float omega)
     s[18] = fmaf(omega, (1.0f / 3.0f) * P - s[18], s[18]);
 }
 
-static float ld16(uint16_t v, int kind) { return kind ? bf16_to_float(v) : half_to_float(v); }
-static uint16_t st16(float v, int kind) { return kind ? float_to_bf16(v) : float_to_half(v); }
+/* IEEE half, rounded toward zero (the truncation of float_to_half's normal
+ * and subnormal cases; finite values beyond the range give the largest
+ * finite half). */
+static uint16_t float_to_half_rz(float f)
+{
+    const uint32_t x = float_to_bits(f);
+    const uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7fffffffu;
+    if (ax > 0x7f800000u) return (uint16_t)(sign | 0x7e00u);
+    if (ax == 0x7f800000u) return (uint16_t)(sign | 0x7c00u);
+    if (ax >= 0x47800000u) return (uint16_t)(sign | 0x7bffu);
+    if (ax >= 0x38800000u) return (uint16_t)(sign | ((((ax >> 23) - 112u) << 10) | ((ax & 0x7fffffu) >> 13)));
+    {
+        const int shift = 126 - (int)(ax >> 23);
+        if (shift > 24) return (uint16_t)sign;
+        return (uint16_t)(sign | (((ax & 0x7fffffu) | 0x800000u) >> shift));
+    }
+}
+
+/* Stochastic-rounding keys of the F16SR mode (kind 2), restating sr_hash and
+ * sr_dither of cavityflow_cuda_gb300/csrc/lbm_core.cuh: the "lowbias32"
+ * integer hash (C. Wellons) of the cell's compact index and the time step,
+ * and 13 dither bits per population from a Weyl sequence started at it. */
+static uint32_t sr_hash(uint32_t cell, uint32_t step)
+{
+    uint32_t x = cell ^ (step * 0x9E3779B9u);
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+static uint32_t sr_dither(uint32_t h, int k) { return (h * 0x2545F491u + (uint32_t)k * 0x9E3779B9u) >> 19; }
+
+/* kind 2 keeps half(s * 2^12): the scale is exact (a power of two). */
+static const float kSrScale = 4096.0f, kSrUnscale = 1.0f / 4096.0f;
+
+static float ld16(uint16_t v, int kind)
+{
+    if (kind == 2) return half_to_float(v) * kSrUnscale;
+    return kind ? bf16_to_float(v) : half_to_float(v);
+}
+/* The time steps work in step units: kind 2's scaled deviations (no scaling
+ * per population), the plain deviation otherwise. */
+static float ld16_step(uint16_t v, int kind) { return kind == 2 ? half_to_float(v) : ld16(v, kind); }
+static int step_log2(int kind) { return kind == 2 ? 12 : 0; }
+/* Lid cells' equilibrium deviation in step units. */
+static void lid_step(float lid_u, int kind, float* f)
+{
+    int k;
+    equilibriumf(0.0f, lid_u, 0.0f, 0.0f, f);
+    if (kind == 2)
+        for (k = 0; k < 19; ++k) f[k] *= kSrScale;
+}
+/* Store of population k (a value in step units) of the cell with hash h:
+ * kind 2 adds the dither below the 13 bits half precision drops and
+ * truncates (stochastic rounding). */
+static uint16_t st16k(float v, int kind, uint32_t h, int k)
+{
+    if (kind == 2) return float_to_half_rz(bits_to_float(float_to_bits(v) + sr_dither(h, k)));
+    return kind ? float_to_bf16(v) : float_to_half(v);
+}
 
 void orc_init_s(uint16_t* dd, int32_t* flags, int nx, int ny, int nz, const int32_t bc[6])
 {
@@ -178,7 +242,7 @@ void orc_init_s(uint16_t* dd, int32_t* flags, int nx, int ny, int nz, const int3
 }
 
 void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                 int kind, const int32_t origin[3], const int32_t size[3])
+                 int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
 {
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
@@ -189,6 +253,7 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
     for (Zi = 0; Zi < size[2]; ++Zi) {
         int Yi, Xi, k;
         float f[19];
+        uint32_t h;
         for (Yi = 0; Yi < size[1]; ++Yi) {
             for (Xi = 0; Xi < size[0]; ++Xi) {
                 const int64_t gid = (origin[2] + Zi) * XY + (origin[1] + Yi) * X + origin[0] + Xi;
@@ -196,22 +261,23 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
                 if (gid >= C) continue;
                 fl = flags[gid];
                 if (fl == ORC_FLUID) {
-                    for (k = 0; k < 19; ++k) f[k] = ld16(dd[k * C + gid], kind);
-                    collide_shifted(f, inv_tau);
+                    for (k = 0; k < 19; ++k) f[k] = ld16_step(dd[k * C + gid], kind);
+                    collide_shifted(f, inv_tau, step_log2(kind));
                 } else if (fl == ORC_VELOCITY_INJECTION) {
-                    equilibriumf(0.0f, lid_u, 0.0f, 0.0f, f);
+                    lid_step(lid_u, kind, f);
                 } else {
                     continue;
                 }
-                for (k = 0; k < 18; ++k) dd[(k ^ 1) * C + gid] = st16(f[k], kind);
-                dd[18 * C + gid] = st16(f[18], kind);
+                h = sr_hash((uint32_t)gid, step);
+                for (k = 0; k < 18; ++k) dd[(k ^ 1) * C + gid] = st16k(f[k], kind, h, k);
+                dd[18 * C + gid] = st16k(f[18], kind, h, 18);
             }
         }
     }
 }
 
 void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                int kind, const int32_t origin[3], const int32_t size[3])
+                int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
 {
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
@@ -224,6 +290,7 @@ void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, floa
     for (Zi = 0; Zi < size[2]; ++Zi) {
         int Yi, Xi, k;
         float f[19];
+        uint32_t h;
         int64_t pos[19];
         for (Yi = 0; Yi < size[1]; ++Yi) {
             for (Xi = 0; Xi < size[0]; ++Xi) {
@@ -234,13 +301,15 @@ void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, floa
                 if (fl == ORC_OBSTACLE) continue;            /* swap then write back: no change */
                 for (k = 0; k < 19; ++k) pos[k] = k * C + (gid + delta[k]) % C;
                 if (fl == ORC_FLUID) {
-                    for (k = 0; k < 18; ++k) f[k ^ 1] = ld16(dd[pos[k]], kind);
-                    f[18] = ld16(dd[pos[18]], kind);
-                    collide_shifted(f, inv_tau);
-                    for (k = 0; k < 19; ++k) dd[pos[k]] = st16(f[k], kind);
+                    for (k = 0; k < 18; ++k) f[k ^ 1] = ld16_step(dd[pos[k]], kind);
+                    f[18] = ld16_step(dd[pos[18]], kind);
+                    collide_shifted(f, inv_tau, step_log2(kind));
+                    h = sr_hash((uint32_t)gid, step);
+                    for (k = 0; k < 19; ++k) dd[pos[k]] = st16k(f[k], kind, h, k);
                 } else if (fl == ORC_VELOCITY_INJECTION) {
-                    equilibriumf(0.0f, lid_u, 0.0f, 0.0f, f);
-                    for (k = 0; k < 19; ++k) dd[pos[k]] = st16(f[k], kind);
+                    lid_step(lid_u, kind, f);
+                    h = sr_hash((uint32_t)gid, step);
+                    for (k = 0; k < 19; ++k) dd[pos[k]] = st16k(f[k], kind, h, k);
                 } else {                                      /* streamed through unchanged */
                     uint16_t raw[19];
                     for (k = 0; k < 18; ++k) raw[k ^ 1] = dd[pos[k]];
@@ -327,5 +396,7 @@ void orc_reduce_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int 
 }
 
 uint16_t orc_float_to_half(float f) { return float_to_half(f); }
+uint16_t orc_float_to_half_rz(float f) { return float_to_half_rz(f); }
+uint32_t orc_sr_hash(uint32_t cell, uint32_t step) { return sr_hash(cell, step); }
 float orc_half_to_float(uint16_t h) { return half_to_float(h); }
 uint16_t orc_float_to_bf16(float f) { return float_to_bf16(f); }

@@ -54,18 +54,21 @@ void orc_macros_f(const float* dd, const int32_t* flags, int nx, int ny, int nz,
 void orc_reduce_f(const float* dd, const int32_t* flags, int nx, int ny, int nz,
                   int last_was_alpha, double out[4]);
 
-/* ---- shifted 16-bit storage (f - w in FP16 when kind = 0, BF16 when kind = 1;
- *      collision in float) -- the GB300 solver's precision extension ---- */
+/* ---- shifted 16-bit storage (f - w in FP16 when kind = 0, BF16 when kind = 1,
+ *      FP16 of (f - w) * 2^12 with stochastic rounding keyed by `step` when
+ *      kind = 2; collision in float) -- the GB300 solver's precision extension ---- */
 void orc_init_s(uint16_t* dd, int32_t* flags, int nx, int ny, int nz, const int32_t bc[6]);
 void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                 int kind, const int32_t origin[3], const int32_t size[3]);
+                 int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
 void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                int kind, const int32_t origin[3], const int32_t size[3]);
+                int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
 void orc_macros_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, int last_was_alpha,
                   float lid_u, int kind, float* rho, float* jx, float* jy, float* jz);
 void orc_reduce_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, int last_was_alpha, int kind,
                   double out[4]);
 uint16_t orc_float_to_half(float f);
+uint16_t orc_float_to_half_rz(float f);
+uint32_t orc_sr_hash(uint32_t cell, uint32_t step);
 float orc_half_to_float(uint16_t h);
 uint16_t orc_float_to_bf16(float f);
 

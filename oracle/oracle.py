@@ -130,7 +130,8 @@ class Oracle(_Lib):
         return out  # mass, px, py, pz
 
     # -- shifted 16-bit storage (the solver's FP16/BF16 extension) --------------
-    # kind 0: FP16, 1: BF16.  Arrays are uint16 bit patterns of f - w.
+    # kind 0: FP16, 1: BF16, 2: FP16 of (f - w) * 2^12 with stochastic
+    # rounding.  Arrays are uint16 bit patterns.
     def init_s(self, nx, ny, nz, bc=(OBSTACLE,) * 6):
         dd = np.zeros((19, nz + 2, ny + 2, nx + 2), dtype=np.uint16)
         flags = np.zeros((nz + 2, ny + 2, nx + 2), dtype=np.int32)
@@ -144,8 +145,9 @@ class Oracle(_Lib):
         origin = (0, 0, 0) if origin is None else origin
         size = (nx + 2, ny + 2, nz + 2) if size is None else size
         fn = self.lib.orc_beta_s if counter & 1 else self.lib.orc_alpha_s
-        fn.argtypes = [_P, _P, _I, _I, _I, C.c_float, C.c_float, _I, _P, _P]
-        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, int(kind), _i3(origin), _i3(size))
+        fn.argtypes = [_P, _P, _I, _I, _I, C.c_float, C.c_float, _I, _P, _P, C.c_uint32]
+        fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, int(kind), _i3(origin), _i3(size),
+           int(counter) & 0xFFFFFFFF)
 
     def run_cavity_s(self, nx, ny, nz, kind, inv_tau, lid_u, steps, lid=True):
         dd, flags = self.init_s(nx, ny, nz)
@@ -159,6 +161,8 @@ class Oracle(_Lib):
         """float32 populations f = s + w of a shifted 16-bit array."""
         if kind == 0:
             f = dd.view(np.float16).astype(np.float32)
+        elif kind == 2:
+            f = dd.view(np.float16).astype(np.float32) * np.float32(1.0 / 4096.0)
         else:
             f = (dd.astype(np.uint32) << 16).view(np.float32)
         w = np.array([np.float32(1) / np.float32(18)] * 4 + [np.float32(1) / np.float32(36)] * 12 +

@@ -79,7 +79,7 @@ def read_vtk(path):
     return out
 
 
-@pytest.mark.parametrize("storage", ["f64", "f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16s", "bf16s", "f16sr"])
 def test_checkpoint_resume_is_bit_identical(gpu, tmp_path, storage):
     from cavityflow_cuda_gb300 import CLbmSolverGB300
 

@@ -9,7 +9,7 @@ from oracle import oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-KIND = {"f16s": 0, "bf16s": 1}
+KIND = {"f16s": 0, "bf16s": 1, "f16sr": 2}
 
 
 def shifted_solver(n, storage, inv_tau, lid, **kw):
@@ -18,7 +18,7 @@ def shifted_solver(n, storage, inv_tau, lid, **kw):
     return CLbmSolverGB300(n, inv_tau, lid, storage=storage, **kw)
 
 
-@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+@pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
 @pytest.mark.parametrize("variant", range(18))
 def test_shifted_storage_matches_oracle(gpu, oracle, storage, variant):
     _, itau = orc.tau_of(0.0192, np.float32)
@@ -42,7 +42,25 @@ def test_shifted_storage_matches_oracle(gpu, oracle, storage, variant):
     assert ran >= 2
 
 
-@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+def test_stochastic_storage_graph_replays_match_oracle(gpu, oracle):
+    """F16SR keys each step's rounding by the step number: a run long enough
+    to replay captured graphs (which rewrite their first step before each
+    replay) equals the oracle, and so do the same steps taken one by one."""
+    _, itau = orc.tau_of(0.0192, np.float32)
+    lid = np.float32(0.08)
+    n, steps = (20, 14, 11), 150
+    dd, _ = oracle.run_cavity_s(*n, 2, itau, lid, steps)
+    want = oracle.unshift(dd, 2)
+    with shifted_solver(n, "f16sr", itau, lid) as s:
+        s.run(steps)
+        assert np.array_equal(s.get_all().view(np.uint32), want.view(np.uint32))
+    with shifted_solver(n, "f16sr", itau, lid) as s:
+        for i in range(steps):
+            (s.simulationStepBeta if i & 1 else s.simulationStepAlpha)()
+        assert np.array_equal(s.get_all().view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
 def test_shifted_macros_and_reduce_match_oracle(gpu, oracle, storage):
     _, itau = orc.tau_of(0.032, np.float32)
     lid = np.float32(0.06)
@@ -62,7 +80,7 @@ def test_shifted_macros_and_reduce_match_oracle(gpu, oracle, storage):
         assert np.allclose(red, want_red, rtol=1e-12, atol=1e-9)
 
 
-@pytest.mark.parametrize("storage", ["f16s", "bf16s"])
+@pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
 def test_shifted_population_roundtrip(gpu, storage):
     """set -> get of populations converts f <-> f - w exactly where 16 bits hold it."""
     rng = np.random.default_rng(5)
@@ -73,7 +91,7 @@ def test_shifted_population_roundtrip(gpu, storage):
         src = (w[:, None, None, None] + 0.001 * rng.standard_normal((19, 3, 4, 5))).astype(np.float32)
         s.setDensityDistributions(src, (2, 2, 2), (5, 4, 3))
         got = s.getDensityDistributions((2, 2, 2), (5, 4, 3))
-        tol = 1e-6 if storage == "f16s" else 1e-5
+        tol = 1e-5 if storage == "bf16s" else 1e-6
         assert np.abs(got - src).max() < tol
 
 
@@ -89,7 +107,7 @@ def test_fp16_velocity_error_against_fp64(gpu):
         s.run(steps)
         u64 = s.getVelocities().astype(np.float64)
     errs = {}
-    for storage in ("f32", "f16s", "bf16s"):
+    for storage in ("f32", "f16s", "bf16s", "f16sr"):
         _, itau = orc.tau_of(0.0512, np.float32)
         with CLbmSolverGB300(n, itau, np.float32(0.1), storage=storage) as s:
             s.run(steps)
@@ -97,4 +115,5 @@ def test_fp16_velocity_error_against_fp64(gpu):
         errs[storage] = np.sqrt(((u - u64) ** 2).sum() / (u64 ** 2).sum())
     assert errs["f32"] < 1e-4, errs   # unshifted FP32 loses digits in f - w itself
     assert errs["f16s"] < 1e-3, errs
+    assert errs["f16sr"] < errs["f16s"], errs  # stochastic rounding removes the bias of rounding to nearest
     print("L2 velocity error vs FP64:", errs)

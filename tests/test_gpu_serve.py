@@ -22,7 +22,7 @@ def _solo(size, nu, lid, steps, storage):
         return s.getDensities(), s.getVelocities()
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16s", "f64"])
+@pytest.mark.parametrize("storage", ["f32", "f16s", "f64", "f16sr"])
 def test_served_results_match_solo_runs(gpu, storage):
     from cavityflow_cuda_gb300 import LbmServer
 

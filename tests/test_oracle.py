@@ -141,7 +141,7 @@ def test_16bit_conversions_round_to_nearest_even(oracle):
                           torch.from_numpy(x).to(torch.bfloat16).view(torch.int16).numpy().view(np.uint16))
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("kind", [0, 1, 2])
 def test_shifted_storage_tracks_fp32(oracle, kind):
     """FP16/BF16 deviation storage follows the FP32 run closely on a small cavity."""
     _, itau = orc.tau_of(0.032, np.float32)
@@ -152,4 +152,63 @@ def test_shifted_storage_tracks_fp32(oracle, kind):
     _, ux, uy, uz = oracle.macros(ref, flags, False, np.float32(0.05))
     _, sx, sy, sz = oracle.macros_s(dd, flags, False, np.float32(0.05), kind)
     err = np.sqrt(((sx - ux) ** 2 + (sy - uy) ** 2 + (sz - uz) ** 2).sum() / (ux ** 2 + uy ** 2 + uz ** 2).sum())
-    assert err < (2e-3 if kind == 0 else 2e-2), err
+    assert err < (2e-2 if kind == 1 else 2e-3), err
+
+
+def _lowbias32(cell, step):
+    """The stochastic-rounding key hash (C. Wellons' lowbias32 of cell ^ step * golden), in Python."""
+    m = 0xFFFFFFFF
+    x = (cell ^ (step * 0x9E3779B9)) & m
+    x ^= x >> 16
+    x = (x * 0x7FEB352D) & m
+    x ^= x >> 15
+    x = (x * 0x846CA68B) & m
+    x ^= x >> 16
+    return x
+
+
+def test_stochastic_rounding_keys_and_truncation(oracle):
+    """The oracle's key hash matches an independent statement of it, and its
+    round-toward-zero half conversion returns the largest-magnitude half not
+    above the value."""
+    import ctypes as C
+
+    lib = oracle.lib
+    lib.orc_sr_hash.argtypes = [C.c_uint32, C.c_uint32]
+    lib.orc_sr_hash.restype = C.c_uint32
+    for cell, step in ((0, 0), (1, 0), (0, 1), (123456, 789), (2 ** 31 + 5, 2 ** 32 - 1)):
+        assert lib.orc_sr_hash(cell, step) == _lowbias32(cell, step)
+    lib.orc_float_to_half_rz.argtypes = [C.c_float]
+    lib.orc_float_to_half_rz.restype = C.c_uint16
+    rng = np.random.default_rng(1)
+    x = np.concatenate([rng.standard_normal(2000).astype(np.float32) * s for s in (1e-7, 1e-5, 1e-2, 1, 3e4)] +
+                       [np.array([0, -0.0, 65504, 65519.99, 70000, 5.96e-8, 2.98e-8], np.float32)])
+    got = np.array([lib.orc_float_to_half_rz(float(v)) for v in x], dtype=np.uint16).view(np.float16)
+    with np.errstate(over="ignore"):
+        near = x.astype(np.float16)
+    want = near.copy()
+    too_big = np.abs(near.astype(np.float64)) > np.abs(x.astype(np.float64))
+    mag = want.view(np.uint16) & 0x7FFF
+    want.view(np.uint16)[too_big] = (want.view(np.uint16)[too_big] & 0x8000) | (mag[too_big] - 1)
+    assert np.array_equal(got.view(np.uint16), want.view(np.uint16))
+
+
+def test_stochastic_rounding_is_unbiased(oracle):
+    """Kind 2's stores average to the exact value: one value between two
+    halves, stored under 20000 keys (cells) of one step, rounds to its two
+    neighbours with a mean within 2 % of a unit of the exact value."""
+    import ctypes as C
+
+    scaled = np.float32(np.float32(1.2345e-3) * 4096)
+    lo = np.float16(scaled)
+    lib = oracle.lib
+    lib.orc_float_to_half_rz.argtypes = [C.c_float]
+    lib.orc_float_to_half_rz.restype = C.c_uint16
+    bits = np.frombuffer(np.float32(scaled).tobytes(), np.uint32)[0]
+    d = np.array([(_lowbias32(c, 7) * 0x2545F491 & 0xFFFFFFFF) >> 19 for c in range(20000)], dtype=np.uint64)
+    stored = np.array([lib.orc_float_to_half_rz(float(np.frombuffer(np.uint32(bits + int(x)).tobytes(), np.float32)[0]))
+                       for x in d], dtype=np.uint16).view(np.float16).astype(np.float64)
+    ulp = float(np.spacing(lo))
+    assert set(np.unique(stored)) <= {float(np.float16(scaled)), float(np.float16(scaled)) - ulp,
+                                      float(np.float16(scaled)) + ulp}
+    assert abs(stored.mean() - float(scaled)) < 0.02 * ulp
