@@ -147,20 +147,26 @@ struct BF16S {
     static constexpr int kStepLog2 = 0;
 };
 
-// Stochastic-rounding keys.  sr_hash mixes a cell's index in the compact
-// (nx+2)(ny+2)(nz+2) layout with the time step (the "lowbias32" integer hash
-// of C. Wellons); sr_dither gives population k of that cell the top 13 bits
-// of a Weyl sequence started at the hash: uniform over [0, 2^13) from cell to
-// cell and step to step.
-__host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t cell, uint32_t step)
+// Stochastic-rounding keys.  sr_hash mixes the compact index of a row's first
+// cell ((nx+2)(ny+2)(nz+2) layout, x = 0) with the time step (the "lowbias32"
+// integer hash of C. Wellons); sr_cell gives cell x of that row its own key,
+// so a thread hashes once for all its cells; sr_dither gives population k of
+// the cell the top 13 bits of a Weyl sequence started at the product of the
+// key and an odd constant: uniform over [0, 2^13) from cell to cell and step
+// to step.
+__host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t row_cell, uint32_t step)
 {
-    uint32_t x = cell ^ (step * 0x9E3779B9u);
+    uint32_t x = row_cell ^ (step * 0x9E3779B9u);
     x ^= x >> 16;
     x *= 0x7FEB352Du;
     x ^= x >> 15;
     x *= 0x846CA68Bu;
     x ^= x >> 16;
     return x;
+}
+__host__ __device__ __forceinline__ uint32_t sr_cell(uint32_t row_hash, int x)
+{
+    return row_hash ^ ((uint32_t)x * 0x85EBCA6Bu);
 }
 __host__ __device__ __forceinline__ uint32_t sr_dither(uint32_t h, int k)
 {

@@ -132,6 +132,7 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
 
     const bool lid = (y == lid_y);
     const T rho0 = St::shifted ? T(0) : T(1);
+    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
     for (int v = 0; v < CPT; ++v) {
         if (x0 + v > g.nx) continue;  // halo/padding lane: slots stay as they are
@@ -141,7 +142,7 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
-        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
+        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
 #pragma unroll
         for (int k = 0; k < Q; ++k) f[opp(k)][v] = store_pop<St>(c[k], h, k);  // population k -> slot opp(k)
     }
@@ -226,6 +227,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
 
     const bool lid = (y == lid_y);
     const T rho0 = St::shifted ? T(0) : T(1);
+    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
     for (int v = 0; v < CPT; ++v) {
         if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
@@ -235,7 +237,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
-        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
+        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
 #pragma unroll
         for (int k = 0; k < Q; ++k) p[k][v] = store_pop<St>(c[k], h, k);  // population k -> slot k at x + c_k
     }
@@ -373,6 +375,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
 
     const bool lid = (y == lid_y);
     const T rho0 = St::shifted ? T(0) : T(1);
+    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
     for (int v = 0; v < CPT; ++v) {
         if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
@@ -382,7 +385,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
-        if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x0 + v, y, z), step);
+        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
 #pragma unroll
         for (int k = 0; k < Q; ++k) p[k][v] = store_pop<St>(c[k], h, k);  // population k -> slot k at x + c_k
     }

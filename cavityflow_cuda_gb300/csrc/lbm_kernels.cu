@@ -58,7 +58,8 @@ __global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t*
         if (kGravity) alpha_gravity(f, T(1), T(prm.gx), T(prm.gy), T(prm.gz));
     }
     uint32_t h = 0;
-    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y, z), step_of<St>(prm.step_base, prm.step_off));
+    if constexpr (St::stochastic)
+        h = sr_cell(sr_hash((uint32_t)g.ref(0, y, z), step_of<St>(prm.step_base, prm.step_off)), x);
 #pragma unroll
     for (int k = 0; k < Q; ++k) dd[opp(k) * g.S + c0] = store_pop<St>(f[k], h, k);
 }
@@ -90,7 +91,8 @@ __global__ void beta_general(typename St::bits* __restrict__ dd, const uint8_t* 
     // GHOST_LAYER (and any other value): streamed through unchanged (a value
     // read from storage is stored back exactly, also by stochastic rounding)
     uint32_t h = 0;
-    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y, z), step_of<St>(prm.step_base, prm.step_off));
+    if constexpr (St::stochastic)
+        h = sr_cell(sr_hash((uint32_t)g.ref(0, y, z), step_of<St>(prm.step_base, prm.step_off)), x);
 #pragma unroll
     for (int k = 0; k < Q; ++k) dd[pos[k]] = store_pop<St>(f[k], h, k);
 }

@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
                     if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
                     uint32_t h = 0;
-                    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y0 + r, z), step);
+                    if constexpr (St::stochastic) h = sr_cell(sr_hash((uint32_t)g.ref(0, y0 + r, z), step), x);
 #pragma unroll
                     for (int k = 0; k < Q; ++k) sb[opp(k) * slot_elems + col] = store_pop<St>(f[k], h, k);
                 } else {
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
                     if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
                     uint32_t h = 0;
-                    if constexpr (St::stochastic) h = sr_hash((uint32_t)g.ref(x, y0 + r, z), step);
+                    if constexpr (St::stochastic) h = sr_cell(sr_hash((uint32_t)g.ref(0, y0 + r, z), step), x);
 #pragma unroll
                     for (int k = 0; k < Q; ++k) sb[k * slot_elems + col + dir_x(k)] = store_pop<St>(f[k], h, k);
                 }

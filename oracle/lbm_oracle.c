@@ -186,10 +186,11 @@ static uint16_t float_to_half_rz(float f)
     }
 }
 
-/* Stochastic-rounding keys of the F16SR mode (kind 2), restating sr_hash and
- * sr_dither of cavityflow_cuda_gb300/csrc/lbm_core.cuh: the "lowbias32"
- * integer hash (C. Wellons) of the cell's compact index and the time step,
- * and 13 dither bits per population from a Weyl sequence started at it. */
+/* Stochastic-rounding keys of the F16SR mode (kind 2), restating sr_hash,
+ * sr_cell and sr_dither of cavityflow_cuda_gb300/csrc/lbm_core.cuh: the
+ * "lowbias32" integer hash (C. Wellons) of the compact index of the row's
+ * first cell and the time step, a per-cell key from it and x, and 13 dither
+ * bits per population from a Weyl sequence. */
 static uint32_t sr_hash(uint32_t cell, uint32_t step)
 {
     uint32_t x = cell ^ (step * 0x9E3779B9u);
@@ -200,6 +201,7 @@ static uint32_t sr_hash(uint32_t cell, uint32_t step)
     x ^= x >> 16;
     return x;
 }
+static uint32_t sr_cell(uint32_t row_hash, int x) { return row_hash ^ ((uint32_t)x * 0x85EBCA6Bu); }
 static uint32_t sr_dither(uint32_t h, int k) { return (h * 0x2545F491u + (uint32_t)k * 0x9E3779B9u) >> 19; }
 
 /* kind 2 keeps half(s * 2^12): the scale is exact (a power of two). */
@@ -268,7 +270,7 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
                 } else {
                     continue;
                 }
-                h = sr_hash((uint32_t)gid, step);
+                h = sr_cell(sr_hash((uint32_t)(gid - (origin[0] + Xi)), step), origin[0] + Xi);
                 for (k = 0; k < 18; ++k) dd[(k ^ 1) * C + gid] = st16k(f[k], kind, h, k);
                 dd[18 * C + gid] = st16k(f[18], kind, h, 18);
             }
@@ -304,11 +306,11 @@ void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, floa
                     for (k = 0; k < 18; ++k) f[k ^ 1] = ld16_step(dd[pos[k]], kind);
                     f[18] = ld16_step(dd[pos[18]], kind);
                     collide_shifted(f, inv_tau, step_log2(kind));
-                    h = sr_hash((uint32_t)gid, step);
+                    h = sr_cell(sr_hash((uint32_t)(gid - (origin[0] + Xi)), step), origin[0] + Xi);
                     for (k = 0; k < 19; ++k) dd[pos[k]] = st16k(f[k], kind, h, k);
                 } else if (fl == ORC_VELOCITY_INJECTION) {
                     lid_step(lid_u, kind, f);
-                    h = sr_hash((uint32_t)gid, step);
+                    h = sr_cell(sr_hash((uint32_t)(gid - (origin[0] + Xi)), step), origin[0] + Xi);
                     for (k = 0; k < 19; ++k) dd[pos[k]] = st16k(f[k], kind, h, k);
                 } else {                                      /* streamed through unchanged */
                     uint16_t raw[19];
