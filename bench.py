@@ -401,6 +401,7 @@ def extensions(a):
     try:
         out["batch_f32"] = batch_measure("f32", a.batch_count, 2000)
         out["batch_f16s"] = batch_measure("f16s", a.batch_count, 2000)
+        out["batch_f16sr"] = batch_measure("f16sr", a.batch_count, 2000)
         out["batch_note"] = "batched MLUPS over the seeded 512-cavity workload; compare with single-domain MLUPS"
     except Exception as e:  # keep the main line whatever happens here
         out["batch_error"] = repr(e)
@@ -428,8 +429,8 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        res = {s: batch_measure(s, a.batch_count, a.batch_steps) for s in ("f32", "f16s")}
-        for s in ("f32", "f16s"):
+        res = {s: batch_measure(s, a.batch_count, a.batch_steps) for s in ("f32", "f16s", "f16sr")}
+        for s in ("f32", "f16s", "f16sr"):
             res[s]["single_domain_384_mlups"] = round(single_measure(s, 384, 400), 1)
             res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s]["single_domain_384_mlups"], 3)
         print(json.dumps({"workload": "batch", "results": res}), flush=True)
@@ -438,7 +439,7 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        res = {s_: serve_measure(s_, a.serve_count, a.serve_step_scale) for s_ in ("f32", "f16s")}
+        res = {s_: serve_measure(s_, a.serve_count, a.serve_step_scale) for s_ in ("f32", "f16s", "f16sr")}
         print(json.dumps({"workload": "serve", "results": res}), flush=True)
         return
     if a.workload == "precision":

@@ -137,7 +137,7 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     if (!b) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
     b->storage = storage;
     b->device = device;
-    b->variant = default_variant(storage) < lbm::kRegisterVariants ? default_variant(storage) : 3;
+    b->variant = default_batch_variant(storage);
     auto bail = [&](int r) { free_batch(b); return r; };
 
     // pool layout: each domain's 19 padded slots, 256-byte aligned

@@ -85,6 +85,18 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
 }  // namespace
 
+// Batches of the seeded 512-cavity workload (edges 16..96) favour 16-byte
+// vectors in both kernels with two-warp blocks (variant 11), FP16 with
+// stochastic rounding the 16-byte alpha / 8-byte beta pair (variant 10).
+int lbm_detail::default_batch_variant(int storage)
+{
+    switch (storage) {
+    case LBM_STORAGE_F64: return 3;
+    case LBM_STORAGE_F16SR: return 10;
+    default: return 11;
+    }
+}
+
 int lbm_detail::default_variant(int storage)
 {
     switch (storage) {

@@ -553,16 +553,28 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
     const uint32_t step = step_of<St>(step_base, step_off);
     using T = typename St::T;
     constexpr int which = kAlpha ? 0 : 1;
-    // Every thread of a CTA walks the same virtual blocks, so the block-wide
-    // barriers of the exchanging beta body are reached uniformly.
-    for (long long vb = blockIdx.x; vb < vblocks; vb += gridDim.x) {
-        int lo = 0, hi = ndom - 1;
+    // Each CTA takes a contiguous run of virtual blocks: one binary search for
+    // the run's first domain, then the domain index only moves forward (a
+    // search per virtual block would put ~log2(ndom) dependent table loads in
+    // front of every block's work).  Every thread of a CTA walks the same
+    // virtual blocks, so the block-wide barriers of the exchanging beta body
+    // are reached uniformly.
+    const long long per_cta = (vblocks + gridDim.x - 1) / gridDim.x;
+    const long long vb_begin = (long long)blockIdx.x * per_cta;
+    const long long vb_end = vb_begin + per_cta < vblocks ? vb_begin + per_cta : vblocks;
+    if (vb_begin >= vb_end) return;
+    int lo = 0;
+    {
+        int hi = ndom - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
-            if (doms[mid].block_start[which] <= vb) lo = mid;
+            if (doms[mid].block_start[which] <= vb_begin) lo = mid;
             else hi = mid - 1;
         }
-        const BatchDomain d = doms[lo];
+    }
+    for (long long vb = vb_begin; vb < vb_end; ++vb) {
+        while (lo + 1 < ndom && doms[lo + 1].block_start[which] <= vb) ++lo;
+        const BatchDomain& d = doms[lo];
         const long long t = (vb - d.block_start[which]) * BLOCK + threadIdx.x;
         const uint32_t ds = step + d.step0;
         if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);

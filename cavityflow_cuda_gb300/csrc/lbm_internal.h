@@ -44,6 +44,8 @@ int cuda_fail(cudaError_t e, const char* what);
 int elem_bytes(int storage);
 int value_bytes(int storage);
 int default_variant(int storage);
+// Default register variant of the batch kernel (many small domains).
+int default_batch_variant(int storage);
 // Creates a solver; with `external_dd` its populations live there (a batch
 // pool) and are initialised but never freed by the solver.
 int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out);

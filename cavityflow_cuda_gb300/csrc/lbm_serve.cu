@@ -296,7 +296,8 @@ int lbm_server_create(const lbm_server_config* cfg, lbm_server** out)
     if (!s) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->cfg = *cfg;
     s->cfg.max_round_steps &= ~1;
-    s->variant = cfg->fast_variant > 0 && cfg->fast_variant <= lbm::kRegisterVariants ? cfg->fast_variant - 1 : 0;
+    s->variant = cfg->fast_variant > 0 && cfg->fast_variant <= lbm::kRegisterVariants ? cfg->fast_variant - 1
+                                                                                       : default_batch_variant(cfg->storage);
     s->arena_bytes = (size_t)((double)cfg->budget_bytes * kArenaShare) / kAlign * kAlign;
     if (s->arena_bytes + (size_t)(1 << 30) > free_b) {
         delete s;
