@@ -182,6 +182,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     const int y = 1 + (int)(row % g.ny);
     const int z = 1 + (int)(row / g.ny);
     const int x0 = 1 + gi * CPT;
+    const long long base = g.idx(x0, y, z);
     // The neighbouring group of the same row is held by the adjacent lane.
     const bool left_in = gi > 0 && lane > 0;
     const bool right_in = gi < G - 1 && lane < 31;
@@ -197,7 +198,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
         bits a[CPT];
         if (active) IO::load_raw(dd + rb, a);
         else {
@@ -245,7 +246,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
         if constexpr (cx == 0) {
             if (active) IO::store_raw(dd + rb, p[k]);
         } else if constexpr (cx == 1) {
@@ -314,6 +315,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
     const int y = 1 + (int)(row % g.ny);
     const int z = 1 + (int)(row / g.ny);
     const int x0 = 1 + gi * CPT;
+    const long long base = g.idx(x0, y, z);
     // The neighbouring group of the same row belongs to thread t -+ 1 of this block.
     const bool left_in = gi > 0 && threadIdx.x > 0;
     const bool right_in = gi < G - 1 && threadIdx.x < BLOCK - 1;
@@ -323,7 +325,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
         IO::load_raw(dd + rb, a[k]);
         ext[k] = bits(0);
         if constexpr (cx == 1) {
@@ -403,7 +405,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
-        const long long rb = k * g.S + g.idx(x0, y + dir_y(k), z + dir_z(k));
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
         if constexpr (cx == 0) {
             if (active) IO::store_raw(dd + rb, p[k]);
         } else if constexpr (cx == 1) {
