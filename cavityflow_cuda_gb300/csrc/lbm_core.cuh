@@ -229,6 +229,33 @@ __device__ __forceinline__ typename St::bits store_pop(typename St::T v, uint32_
     else return St::store(v);
 }
 
+// Unsigned 32-bit division by a divisor fixed at launch, as a multiply-high
+// and shifts (the round-up method of Granlund and Montgomery, 1994): with
+// l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1, every n < 2^32 has
+// n / d = (t + ((n - t) >> 1)) >> (l - 1), t = mulhi(n, m); d = 1 is n.
+struct FastDiv {
+    uint32_t d = 1, m = 0;
+    int l = 0;
+    static FastDiv make(uint32_t d)
+    {
+        FastDiv f;
+        f.d = d;
+        if (d > 1) {
+            int l = 0;
+            while ((1ull << l) < d) ++l;
+            f.l = l;
+            f.m = (uint32_t)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+        }
+        return f;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const
+    {
+        if (l == 0) return n;
+        const uint32_t t = __umulhi(n, m);
+        return (t + ((n - t) >> 1)) >> (l - 1);
+    }
+};
+
 // Scalar lattice parameters of one domain, and the time step of the next
 // launch, *step_base + step_off (it keys stochastic rounding; step_base points
 // to device memory so that captured graphs can be replayed at later steps).

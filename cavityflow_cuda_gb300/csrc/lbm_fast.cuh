@@ -106,23 +106,63 @@ __device__ __forceinline__ B shfl_down_bits(B v, int d)
     else return __shfl_down_sync(0xffffffffu, v, d);
 }
 
-// Alpha step of the CPT cells owned by thread index t of one domain (t runs
-// over groups x rows x planes: t = ((z-1) * ny + (y-1)) * G + group).
+// The group of CPT cells a thread owns: group gi of row y of plane z.  An
+// inactive thread (past the end) carries a valid group (it reads, never
+// writes).
+struct Cells {
+    int gi, y, z;
+    bool active;
+};
+
+// From a thread index t over groups x rows x planes of one domain,
+// t = ((z-1) * ny + (y-1)) * G + gi (the batch kernel's virtual blocks).
+template <int CPT>
+__device__ __forceinline__ Cells cells_of_index(const Grid& g, long long t)
+{
+    const int G = (g.nx + CPT - 1) / CPT;
+    const long long total = (long long)G * g.ny * g.nz;
+    Cells c;
+    c.active = t < total;
+    const long long tt = c.active ? t : 0;
+    if (total <= 0xffffffffll) {  // 32-bit division is far cheaper than 64-bit
+        const uint32_t u = (uint32_t)tt, row = u / (uint32_t)G;
+        c.gi = (int)(u - row * (uint32_t)G);
+        c.y = 1 + (int)(row % (uint32_t)g.ny);
+        c.z = 1 + (int)(row / (uint32_t)g.ny);
+    } else {
+        const long long row = tt / G;
+        c.gi = (int)(tt - row * G);
+        c.y = 1 + (int)(row % g.ny);
+        c.z = 1 + (int)(row / g.ny);
+    }
+    return c;
+}
+
+// From an index i over the G * ny groups of plane z (the step kernels' grid:
+// x over a plane's groups, y over planes); divG divides by G.
+__device__ __forceinline__ Cells cells_of_plane(const Grid& g, int G, const FastDiv& divG, uint32_t i, int z)
+{
+    Cells c;
+    c.active = i < (uint32_t)G * (uint32_t)g.ny;
+    const uint32_t ii = c.active ? i : 0u;
+    const uint32_t row = divG.div(ii);
+    c.gi = (int)(ii - row * (uint32_t)G);
+    c.y = 1 + (int)row;
+    c.z = z;
+    return c;
+}
+
+// Alpha step of the CPT cells of group `c`.
 template <class St, int CPT>
 __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                             const typename St::T inv_tau, const typename St::T lid_u,
-                                            const int lid_y, const long long t, const uint32_t step)
+                                            const int lid_y, const Cells c, const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
     using IO = Vio<St, CPT>;
-    const int G = (g.nx + CPT - 1) / CPT;
-    const long long total = (long long)G * g.ny * g.nz;
-    if (t >= total) return;
-    const int gi = (int)(t % G);
-    const long long row = t / G;
-    const int y = 1 + (int)(row % g.ny);
-    const int z = 1 + (int)(row / g.ny);
+    if (!c.active) return;
+    const int gi = c.gi, y = c.y, z = c.z;
     const int x0 = 1 + gi * CPT;
     const long long base = g.idx(x0, y, z);
 
@@ -155,32 +195,29 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
                                                           const typename St::T inv_tau,
                                                           const typename St::T lid_u, const int lid_y,
                                                           const uint32_t* __restrict__ step_base,
-                                                          const uint32_t step_off)
+                                                          const uint32_t step_off, const FastDiv divG,
+                                                          const int z_base)
 {
-    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
+    const int G = (g.nx + CPT - 1) / CPT;
+    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+                         cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
                          step_of<St>(step_base, step_off));
 }
 
-// Beta step of the CPT cells owned by thread index t of one domain.  All 32
-// lanes of the warp must call it together, with consecutive t (they exchange
-// edge elements by shuffles); lanes past the domain's end take part in the
-// shuffles only.
+// Beta step of the CPT cells of group `c`.  All 32 lanes of the warp must
+// call it together, with consecutive groups (they exchange edge elements by
+// shuffles); lanes past the domain's end take part in the shuffles only.
 template <class St, int CPT>
 __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                            const typename St::T inv_tau, const typename St::T lid_u,
-                                           const int lid_y, const long long t, const uint32_t step)
+                                           const int lid_y, const Cells c, const uint32_t step)
 {
     using T = typename St::T;
     using IO = Vio<St, CPT>;
     const int G = (g.nx + CPT - 1) / CPT;
-    const long long total = (long long)G * g.ny * g.nz;
-    const bool active = t < total;
+    const bool active = c.active;
     const int lane = threadIdx.x & 31;
-    const long long tt = active ? t : 0;
-    const int gi = (int)(tt % G);
-    const long long row = tt / G;
-    const int y = 1 + (int)(row % g.ny);
-    const int z = 1 + (int)(row / g.ny);
+    const int gi = c.gi, y = c.y, z = c.z;
     const int x0 = 1 + gi * CPT;
     const long long base = g.idx(x0, y, z);
     // The neighbouring group of the same row is held by the adjacent lane.
@@ -290,11 +327,11 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
 // barriers), so only lanes at a row edge or at the block's two ends touch the
 // odd element with a scalar access; every other thread issues exactly 19
 // vector loads and 19 vector stores, as in alpha.  All BLOCK threads of the
-// block must call it together, with consecutive t.
+// block must call it together, with consecutive groups.
 template <class St, int CPT, int BLOCK>
 __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ dd, const Grid& g,
                                                const typename St::T inv_tau, const typename St::T lid_u,
-                                               const int lid_y, const long long t, const uint32_t step)
+                                               const int lid_y, const Cells c, const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -305,15 +342,10 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
     // after it (s_head, s_tail).
     __shared__ bits s_first[W][6], s_last[W][6], s_head[W][6], s_tail[W][6];
     const int G = (g.nx + CPT - 1) / CPT;
-    const long long total = (long long)G * g.ny * g.nz;
-    const bool active = t < total;
+    const bool active = c.active;  // inactive lanes read a valid cell, never write
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const long long tt = active ? t : 0;  // inactive lanes read a valid cell, never write
-    const int gi = (int)(tt % G);
-    const long long row = tt / G;
-    const int y = 1 + (int)(row % g.ny);
-    const int z = 1 + (int)(row / g.ny);
+    const int gi = c.gi, y = c.y, z = c.z;
     const int x0 = 1 + gi * CPT;
     const long long base = g.idx(x0, y, z);
     // The neighbouring group of the same row belongs to thread t -+ 1 of this block.
@@ -450,21 +482,28 @@ template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_blk(typename St::bits* __restrict__ dd, const Grid g,
                                                              const typename St::T inv_tau,
                                                              const typename St::T lid_u, const int lid_y,
-                                                          const uint32_t* __restrict__ step_base,
-                                                          const uint32_t step_off)
+                                                             const uint32_t* __restrict__ step_base,
+                                                             const uint32_t step_off, const FastDiv divG,
+                                                             const int z_base)
 {
-    beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
-                                   step_of<St>(step_base, step_off));
+    const int G = (g.nx + CPT - 1) / CPT;
+    beta_cells_blk<St, CPT, BLOCK>(
+        dd, g, inv_tau, lid_u, lid_y,
+        cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
+        step_of<St>(step_base, step_off));
 }
 
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                          const typename St::T inv_tau,
                                                          const typename St::T lid_u, const int lid_y,
-                                                          const uint32_t* __restrict__ step_base,
-                                                          const uint32_t step_off)
+                                                         const uint32_t* __restrict__ step_base,
+                                                         const uint32_t step_off, const FastDiv divG,
+                                                         const int z_base)
 {
-    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, (long long)blockIdx.x * BLOCK + threadIdx.x,
+    const int G = (g.nx + CPT - 1) / CPT;
+    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+                        cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
                         step_of<St>(step_base, step_off));
 }
 
@@ -482,26 +521,32 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
     using T = typename St::T;
     constexpr FastVariant fv = kFastMenu[VARIANT];
     auto* d = static_cast<typename St::bits*>(dd);
+    // grid: x over the groups of one plane, y over planes (in chunks of at most
+    // 65535 planes, the grid's y limit)
+    constexpr int kMaxPlanes = 65535;
+    auto launch = [&](auto kern, int CPT, int block) -> cudaError_t {
+        const int G = (g.nx + CPT - 1) / CPT;
+        const long long per_plane = (long long)G * g.ny;
+        if (per_plane > 0xffffffffll) return cudaErrorInvalidValue;
+        const FastDiv divG = FastDiv::make((uint32_t)G);
+        const unsigned bx = (unsigned)((per_plane + block - 1) / block);
+        for (int z0 = 0; z0 < g.nz; z0 += kMaxPlanes) {
+            const int planes = g.nz - z0 < kMaxPlanes ? g.nz - z0 : kMaxPlanes;
+            kern<<<dim3(bx, (unsigned)planes), block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base,
+                                                               p.step_off, divG, z0);
+            if (z0 > 0) add_launches(1);
+        }
+        return cudaGetLastError();
+    };
     if (alpha) {
         constexpr KernelShape k = fv.alpha;
         constexpr int CPT = shape_cpt<St>(k);
-        const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
-        const int blocks = (int)((threads + k.block - 1) / k.block);
-        alpha_fast<St, CPT, k.block, k.minb>
-            <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
-    } else {
-        constexpr KernelShape k = fv.beta;
-        constexpr int CPT = shape_cpt<St>(k);
-        const long long threads = (long long)((g.nx + CPT - 1) / CPT) * g.ny * g.nz;
-        const int blocks = (int)((threads + k.block - 1) / k.block);
-        if constexpr (fv.block_exchange)
-            beta_fast_blk<St, CPT, k.block, k.minb>
-                <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
-        else
-            beta_fast<St, CPT, k.block, k.minb>
-                <<<blocks, k.block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base, p.step_off);
+        return launch(alpha_fast<St, CPT, k.block, k.minb>, CPT, k.block);
     }
-    return cudaGetLastError();
+    constexpr KernelShape k = fv.beta;
+    constexpr int CPT = shape_cpt<St>(k);
+    if constexpr (fv.block_exchange) return launch(beta_fast_blk<St, CPT, k.block, k.minb>, CPT, k.block);
+    else return launch(beta_fast<St, CPT, k.block, k.minb>, CPT, k.block);
 }
 
 template <class St, size_t... I>
@@ -578,11 +623,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         while (lo + 1 < ndom && doms[lo + 1].block_start[which] <= vb) ++lo;
         const BatchDomain& d = doms[lo];
         const long long t = (vb - d.block_start[which]) * BLOCK + threadIdx.x;
+        const Cells c = cells_of_index<CPT>(d.g, t);
         const uint32_t ds = step + d.step0;
-        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
+        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
         else if constexpr (kExchange)
-            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
-        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, t, ds);
+            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
+        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
     }
 }
 
