@@ -81,7 +81,8 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // Default launch variant per storage (index into kFastMenu), from kernel
 // timings of the 384^3 cavity on GB300: two-warp blocks with the block-wide
 // beta exchange; FP32 with 8-byte vectors in both kernels, FP16 with a 16-byte
-// alpha and an 8-byte beta, BF16 with 16-byte vectors in both.  FP64 is bound
+// alpha and an 8-byte beta, BF16 with 16-byte vectors in both, FP16 with
+// stochastic rounding 8-byte vectors in four-warp blocks.  FP64 is bound
 // by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
 }  // namespace
 
@@ -103,7 +104,7 @@ int lbm_detail::default_variant(int storage)
     case LBM_STORAGE_F32: return 8;
     case LBM_STORAGE_F16S: return 10;
     case LBM_STORAGE_BF16S: return 11;
-    case LBM_STORAGE_F16SR: return 10;
+    case LBM_STORAGE_F16SR: return 9;
     default: return 3;
     }
 }

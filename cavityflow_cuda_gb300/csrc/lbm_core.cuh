@@ -151,9 +151,9 @@ struct BF16S {
 // cell ((nx+2)(ny+2)(nz+2) layout, x = 0) with the time step (the "lowbias32"
 // integer hash of C. Wellons); sr_cell gives cell x of that row its own key,
 // so a thread hashes once for all its cells; sr_dither gives population k of
-// the cell the top 13 bits of a Weyl sequence started at the product of the
-// key and an odd constant: uniform over [0, 2^13) from cell to cell and step
-// to step.
+// the cell the key's top 13 bits XOR a fixed 13-bit constant of k (a Weyl
+// sequence): uniform over [0, 2^13) from cell to cell and step to step, at
+// one logic operation per population.
 __host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t row_cell, uint32_t step)
 {
     uint32_t x = row_cell ^ (step * 0x9E3779B9u);
@@ -166,11 +166,11 @@ __host__ __device__ __forceinline__ uint32_t sr_hash(uint32_t row_cell, uint32_t
 }
 __host__ __device__ __forceinline__ uint32_t sr_cell(uint32_t row_hash, int x)
 {
-    return row_hash ^ ((uint32_t)x * 0x85EBCA6Bu);
+    return (row_hash ^ ((uint32_t)x * 0x85EBCA6Bu)) * 0x2545F491u;
 }
 __host__ __device__ __forceinline__ uint32_t sr_dither(uint32_t h, int k)
 {
-    return (h * 0x2545F491u + (uint32_t)k * 0x9E3779B9u) >> 19;
+    return (h >> 19) ^ (((uint32_t)(k + 1) * 0x9E3779B9u) >> 19);
 }
 
 // IEEE half deviations scaled by 2^kF16SRScale, rounded stochastically.

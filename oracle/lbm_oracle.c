@@ -189,8 +189,9 @@ static uint16_t float_to_half_rz(float f)
 /* Stochastic-rounding keys of the F16SR mode (kind 2), restating sr_hash,
  * sr_cell and sr_dither of cavityflow_cuda_gb300/csrc/lbm_core.cuh: the
  * "lowbias32" integer hash (C. Wellons) of the compact index of the row's
- * first cell and the time step, a per-cell key from it and x, and 13 dither
- * bits per population from a Weyl sequence. */
+ * first cell and the time step, a per-cell key from it and x (mixed by an
+ * odd multiplier), and 13 dither bits per population: the key's top 13 bits
+ * XOR a 13-bit Weyl-sequence constant of the population. */
 static uint32_t sr_hash(uint32_t cell, uint32_t step)
 {
     uint32_t x = cell ^ (step * 0x9E3779B9u);
@@ -201,8 +202,8 @@ static uint32_t sr_hash(uint32_t cell, uint32_t step)
     x ^= x >> 16;
     return x;
 }
-static uint32_t sr_cell(uint32_t row_hash, int x) { return row_hash ^ ((uint32_t)x * 0x85EBCA6Bu); }
-static uint32_t sr_dither(uint32_t h, int k) { return (h * 0x2545F491u + (uint32_t)k * 0x9E3779B9u) >> 19; }
+static uint32_t sr_cell(uint32_t row_hash, int x) { return (row_hash ^ ((uint32_t)x * 0x85EBCA6Bu)) * 0x2545F491u; }
+static uint32_t sr_dither(uint32_t h, int k) { return (h >> 19) ^ (((uint32_t)(k + 1) * 0x9E3779B9u) >> 19); }
 
 /* kind 2 keeps half(s * 2^12): the scale is exact (a power of two). */
 static const float kSrScale = 4096.0f, kSrUnscale = 1.0f / 4096.0f;
