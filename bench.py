@@ -533,7 +533,7 @@ def run_gpu(a):
         achieved = algo / (avg[dom] / 1e3) / 1e9
         info = s.info()
         kname = f"{dom}_fast" + ("_blk" if dom == "beta" and info["beta_block_exchange"] else "")
-        if info["fast_variant"] >= 12:
+        if info["fast_variant"] >= 13:  # the bulk-copy variants follow the 13 register variants
             kname = "step_tma"
         traffic = profile_traffic(a, kname)
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

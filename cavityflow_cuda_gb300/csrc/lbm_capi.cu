@@ -82,7 +82,8 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // timings of the 384^3 cavity on GB300: two-warp blocks with the block-wide
 // beta exchange; FP32 with 8-byte vectors in both kernels, FP16 with a 16-byte
 // alpha and an 8-byte beta, BF16 with 16-byte vectors in both, FP16 with
-// stochastic rounding 8-byte vectors in four-warp blocks.  FP64 is bound
+// stochastic rounding a 16-byte two-warp alpha and an 8-byte four-warp beta
+// (its beta issues the most instructions per byte).  FP64 is bound
 // by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
 }  // namespace
 
@@ -104,7 +105,7 @@ int lbm_detail::default_variant(int storage)
     case LBM_STORAGE_F32: return 8;
     case LBM_STORAGE_F16S: return 10;
     case LBM_STORAGE_BF16S: return 11;
-    case LBM_STORAGE_F16SR: return 9;
+    case LBM_STORAGE_F16SR: return 12;
     default: return 3;
     }
 }
@@ -661,6 +662,7 @@ int lbm_synchronize(lbm_solver* s)
 }
 
 int lbm_fast_variant_count(void) { return lbm::kFastVariantCount; }
+int lbm_register_variant_count(void) { return lbm::kRegisterVariants; }
 
 int lbm_set_fast_variant(lbm_solver* s, int32_t variant)
 {

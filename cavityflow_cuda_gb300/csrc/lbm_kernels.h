@@ -56,7 +56,7 @@ struct FastVariant {
     KernelShape beta;
     bool block_exchange;
 };
-constexpr int kRegisterVariants = 12;
+constexpr int kRegisterVariants = 13;
 constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
     {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
@@ -70,6 +70,7 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{2, 128, 4}, {2, 128, 4}, true},   // 8-byte vectors, four-warp blocks, block exchange
     {{1, 64, 4}, {2, 64, 8}, true},     // alpha 16-byte, beta 8-byte vectors, block exchange
     {{1, 64, 4}, {1, 64, 4}, true},     // 16-byte vectors, two-warp blocks, block exchange
+    {{1, 64, 4}, {2, 128, 4}, true},    // alpha 16-byte two-warp, beta 8-byte four-warp blocks
 };
 struct TmaConfig {
     int rows;            // rows per work unit

@@ -107,6 +107,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_run": ([V, I64, P], I),
         "lbm_synchronize": ([V], I),
         "lbm_fast_variant_count": ([], I),
+        "lbm_register_variant_count": ([], I),
         "lbm_set_fast_variant": ([V, C.c_int32], I),
         "lbm_autotune": ([V, C.c_int32, P, P], I),
         "lbm_get_density_distributions": ([V, P, P, P, P], I),
@@ -496,7 +497,7 @@ class LbmBatch:
         _check(self._lib.lbm_batch_set_fast_variant(self._h, int(variant)))
 
     def autotune(self, pairs: int = 5):
-        ms = (C.c_float * 12)()
+        ms = (C.c_float * self._lib.lbm_register_variant_count())()
         best = C.c_int32()
         _check(self._lib.lbm_batch_autotune(self._h, int(pairs), C.byref(best), ms))
         return best.value, list(ms)

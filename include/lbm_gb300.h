@@ -256,12 +256,14 @@ int lbm_synchronize(lbm_solver* solver);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: 12 register-blocked
- * vector kernels (0..11: cells per thread, threads per block and blocks per
+/* Number of launch variants of the box-cavity kernels: 13 register-blocked
+ * vector kernels (0..12: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
  * elements per warp or per block) and 6 row-pipelined bulk-copy kernels
- * (12..17: rows per unit, buffers, consumer warps). */
+ * (13..18: rows per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
+/* Number of register variants (the first variants; the batch kernel's menu). */
+int lbm_register_variant_count(void);
 /* Selects a variant for subsequent steps; LBM_ERR_UNSUPPORTED if it needs more
  * shared memory than this domain allows. */
 int lbm_set_fast_variant(lbm_solver* solver, int32_t variant);
@@ -403,11 +405,11 @@ int lbm_batch_get_info(const lbm_batch* batch, lbm_batch_info* info);
 int lbm_batch_domain(lbm_batch* batch, int32_t index, lbm_solver** view);
 /* `steps` steps of every domain (alpha on even counters, beta on odd). */
 int lbm_batch_run(lbm_batch* batch, int64_t steps, void* stream);
-/* Selects a launch variant (0..11, the register variants) for the batch kernel. */
+/* Selects a launch variant (a register variant) for the batch kernel. */
 int lbm_batch_set_fast_variant(lbm_batch* batch, int32_t variant);
 /* Times each register variant on the whole batch (`pairs` alpha/beta pairs,
  * CUDA events), keeps the fastest and restores the populations.  ms_per_pair
- * (optional) receives 12 times.  Synchronous. */
+ * (optional) receives lbm_register_variant_count() times.  Synchronous. */
 int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms_per_pair);
 
 /* ---- servers: cavity-solve requests with continuous batching ---------------

@@ -91,7 +91,7 @@ def test_odd_shapes_match_oracle(gpu, oracle, dtype, n, steps):
         assert same_bits(s.get_all(), want)
 
 
-@pytest.mark.parametrize("variant", range(18))
+@pytest.mark.parametrize("variant", range(19))
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_every_launch_variant_matches_oracle(gpu, oracle, variant, dtype):
     """Each launch variant: register-blocked vector kernels (0-11; 8-11 with
