@@ -19,10 +19,9 @@ cudaError_t launch_tma_f16sr(bool alpha, void* dd, const Grid& g, const Params& 
     return launch_tma_impl<F16SR>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
 }
 
-cudaError_t launch_batch_f16sr(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_f16sr(int variant, bool alpha, const BatchArgs& a, cudaStream_t st)
 {
-    return launch_batch_menu<F16SR>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    return launch_batch_menu<F16SR>(variant, alpha, a, st);
 }
 
 }  // namespace lbm

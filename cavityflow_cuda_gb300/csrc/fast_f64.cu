@@ -19,10 +19,9 @@ cudaError_t launch_tma_f64(bool alpha, void* dd, const Grid& g, const Params& p,
     return launch_tma_impl<F64>(alpha, dd, g, p, lid_y, rows, stages, consumer_warps, err, st);
 }
 
-cudaError_t launch_batch_f64(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                             long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_f64(int variant, bool alpha, const BatchArgs& a, cudaStream_t st)
 {
-    return launch_batch_menu<F64>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    return launch_batch_menu<F64>(variant, alpha, a, st);
 }
 
 }  // namespace lbm

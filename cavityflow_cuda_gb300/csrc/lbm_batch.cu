@@ -41,6 +41,8 @@ struct lbm_batch {
     lbm::BatchDomain* dtable = nullptr;
     uint32_t* step_words = nullptr;  // [0] first step of a graph replay, [1] zero
     long long vblocks[2] = {0, 0};  // virtual blocks of the alpha and the beta kernel
+    int* vb_map[2] = {nullptr, nullptr};  // domain of each virtual block, per kernel
+    long long vb_cap[2] = {0, 0};
     long long interior_cells = 0;
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -58,7 +60,8 @@ void drop_batch_graph(lbm_batch* b)
     }
 }
 
-// Numbers the virtual blocks of the current variant and uploads the table.
+// Numbers the virtual blocks of the current variant, uploads the table and
+// rebuilds the virtual-block maps.
 int build_table(lbm_batch* b)
 {
     for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
@@ -67,16 +70,30 @@ int build_table(lbm_batch* b)
             lbm::BatchDomain& d = b->table[i];
             int cpt = 1, block = 1;
             lbm::fast_variant_shape(b->storage, b->variant, kind == 0, d.g.nx, cpt, block);
-            const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
+            const long long n = lbm::set_batch_shape(d, kind, cpt, block);
+            if (n < 0) return fail(LBM_ERR_INVALID_ARGUMENT, "batch domain %zu is too large", i);
             d.block_start[kind] = next;
             d.step0 = 0;  // every domain is at the batch's step
-            next += (groups + block - 1) / block;
+            next += n;
         }
         b->vblocks[kind] = next;
     }
+    drop_batch_graph(b);
+    CK(cudaDeviceSynchronize(), "batch table (pending work)");
     CK(cudaMemcpy(b->dtable, b->table.data(), b->table.size() * sizeof(lbm::BatchDomain), cudaMemcpyHostToDevice),
        "cudaMemcpy batch table");
-    drop_batch_graph(b);
+    for (int kind = 0; kind < 2; ++kind) {
+        if (b->vblocks[kind] > b->vb_cap[kind]) {
+            if (b->vb_map[kind]) cudaFree(b->vb_map[kind]);
+            b->vb_map[kind] = nullptr;
+            b->vb_cap[kind] = 0;
+            CK(cudaMalloc(&b->vb_map[kind], (size_t)b->vblocks[kind] * sizeof(int)), "cudaMalloc batch block map");
+            b->vb_cap[kind] = b->vblocks[kind];
+        }
+        CK(lbm::launch_batch_map(b->dtable, (int)b->views.size(), b->vblocks[kind], kind, b->vb_map[kind], 0),
+           "batch block map");
+    }
+    CK(cudaDeviceSynchronize(), "batch block map");
     return LBM_OK;
 }
 
@@ -85,8 +102,10 @@ int build_table(lbm_batch* b)
 cudaError_t batch_launch(lbm_batch* b, int variant, bool alpha, cudaStream_t st, uint32_t step_off,
                          bool in_graph = false)
 {
-    return lbm::launch_batch_step(b->storage, variant, alpha, b->pool, b->dtable, (int)b->views.size(),
-                                  b->vblocks[alpha ? 0 : 1], b->step_words + (in_graph ? 0 : 1), step_off, st);
+    const int kind = alpha ? 0 : 1;
+    const lbm::BatchArgs a{b->pool, b->dtable, b->vb_map[kind], b->vblocks[kind], b->step_words + (in_graph ? 0 : 1),
+                           step_off};
+    return lbm::launch_batch_step(b->storage, variant, alpha, a, st);
 }
 
 void sync_views(lbm_batch* b)
@@ -109,6 +128,8 @@ void free_batch(lbm_batch* b)
     }
     if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
     if (b->dtable) cudaFree(b->dtable);
+    for (int kind = 0; kind < 2; ++kind)
+        if (b->vb_map[kind]) cudaFree(b->vb_map[kind]);
     if (b->step_words) cudaFree(b->step_words);
     if (b->pool) cudaFree(b->pool);
     delete b;
@@ -212,7 +233,8 @@ int lbm_batch_get_info(const lbm_batch* b, lbm_batch_info* info)
     lbm::fast_variant_shape(b->storage, b->variant, false, 1, info->beta_cells_per_thread, info->beta_block_threads);
     info->interior_cells = b->interior_cells;
     info->step_counter = b->counter;
-    int64_t bytes = (int64_t)b->pool_bytes + (int64_t)(b->table.size() * sizeof(lbm::BatchDomain));
+    int64_t bytes = (int64_t)b->pool_bytes + (int64_t)(b->table.size() * sizeof(lbm::BatchDomain)) +
+                    (int64_t)((b->vb_cap[0] + b->vb_cap[1]) * (long long)sizeof(int));
     for (const lbm_solver* v : b->views) bytes += v->device_bytes;
     info->device_bytes = bytes;
     return LBM_OK;

@@ -87,14 +87,17 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
 }  // namespace
 
-// Batches of the seeded 512-cavity workload (edges 16..96) favour 16-byte
-// vectors in both kernels with two-warp blocks (variant 11), FP16 with
-// stochastic rounding the 16-byte alpha / 8-byte beta pair (variant 10).
+// Batches of the seeded 512-cavity workload (edges 16..96) favour two-warp
+// alpha blocks with the block-wide beta exchange: FP32 16-byte vectors in both
+// kernels (variant 11), FP16 a 16-byte alpha with an 8-byte four-warp beta
+// (variant 12), FP16 with stochastic rounding 8-byte vectors in four-warp
+// blocks (variant 9).
 int lbm_detail::default_batch_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F64: return 3;
-    case LBM_STORAGE_F16SR: return 10;
+    case LBM_STORAGE_F16S: return 12;
+    case LBM_STORAGE_F16SR: return 9;
     default: return 11;
     }
 }

@@ -580,50 +580,99 @@ namespace lbm {
 // kernels, so a domain's result does not depend on its neighbours in the
 // batch.
 // ---------------------------------------------------------------------------
-struct BatchDomain {
+struct alignas(16) BatchDomain {
     Grid g;
-    long long offset;       // elements from the pool base
+    long long offset;          // elements from the pool base
     double inv_tau;
     double lid_u;
     int lid_y;
-    long long block_start[2];  // first virtual block of this domain: [0] alpha, [1] beta kernel
     uint32_t step0;            // added to the launch's step: this domain's own step count
+    long long block_start[2];  // first virtual block of this domain: [0] alpha, [1] beta kernel
+    FastDiv div_g[2];          // division by the groups per row of the alpha / beta shape
+    FastDiv div_ny;            // division by ny
 };
+static_assert(sizeof(BatchDomain) % 16 == 0, "descriptors are copied in 16-byte chunks");
 
+// Fills the virtual-block geometry of kernel `kind` (0 alpha, 1 beta) for a
+// shape of `cpt` cells per thread and `block` threads, and returns the
+// domain's number of virtual blocks, or -1 if its thread index would not fit
+// 32 bits (the batch kernel divides 32-bit thread indices).
+inline long long set_batch_shape(BatchDomain& d, int kind, int cpt, int block)
+{
+    const long long G = (d.g.nx + cpt - 1) / cpt;
+    const long long threads = G * d.g.ny * d.g.nz;
+    const long long blocks = (threads + block - 1) / block;
+    if (blocks * block >= (1ll << 32)) return -1;
+    d.div_g[kind] = FastDiv::make((uint32_t)G);
+    d.div_ny = FastDiv::make((uint32_t)d.g.ny);
+    return blocks;
+}
+
+// The group of thread t of a domain's virtual blocks, t = ((z-1) * ny +
+// (y-1)) * G + gi; threads past the last group get a valid group, inactive.
+__device__ __forceinline__ Cells cells_of_vblock(const BatchDomain& d, int which, uint32_t t)
+{
+    const FastDiv& dg = d.div_g[which];
+    const uint32_t row = dg.div(t);
+    const uint32_t zz = d.div_ny.div(row);
+    Cells c;
+    c.active = zz < (uint32_t)d.g.nz;
+    c.gi = c.active ? (int)(t - row * dg.d) : 0;
+    c.y = c.active ? 1 + (int)(row - zz * (uint32_t)d.g.ny) : 1;
+    c.z = c.active ? 1 + (int)zz : 1;
+    return c;
+}
+
+// 16-byte asynchronous global -> shared copies (cp.async, no registers held
+// while in flight).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Persistent batch step.  CTA i walks virtual blocks i, i + grid, ... (so the
+// resident CTAs work on one compact front of the pool, as a plain grid would).
+// The descriptor of the next virtual block's domain is copied into shared
+// memory (cp.async) while the current one is processed, so a block starts
+// without a dependent table lookup; one block barrier per virtual block
+// publishes it and keeps the other buffer from being overwritten while read.
+// Every thread of a CTA walks the same virtual blocks, so that barrier and
+// the block-wide barriers of the exchanging beta body are reached uniformly.
 template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, bool kExchange>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
-                                                          const BatchDomain* __restrict__ doms, const int ndom,
+                                                          const BatchDomain* __restrict__ doms,
+                                                          const int* __restrict__ vb_dom,
                                                           const long long vblocks,
                                                           const uint32_t* __restrict__ step_base,
                                                           const uint32_t step_off)
 {
-    const uint32_t step = step_of<St>(step_base, step_off);
     using T = typename St::T;
     constexpr int which = kAlpha ? 0 : 1;
-    // Each CTA takes a contiguous run of virtual blocks: one binary search for
-    // the run's first domain, then the domain index only moves forward (a
-    // search per virtual block would put ~log2(ndom) dependent table loads in
-    // front of every block's work).  Every thread of a CTA walks the same
-    // virtual blocks, so the block-wide barriers of the exchanging beta body
-    // are reached uniformly.
-    const long long per_cta = (vblocks + gridDim.x - 1) / gridDim.x;
-    const long long vb_begin = (long long)blockIdx.x * per_cta;
-    const long long vb_end = vb_begin + per_cta < vblocks ? vb_begin + per_cta : vblocks;
-    if (vb_begin >= vb_end) return;
-    int lo = 0;
-    {
-        int hi = ndom - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (doms[mid].block_start[which] <= vb_begin) lo = mid;
-            else hi = mid - 1;
-        }
-    }
-    for (long long vb = vb_begin; vb < vb_end; ++vb) {
-        while (lo + 1 < ndom && doms[lo + 1].block_start[which] <= vb) ++lo;
-        const BatchDomain& d = doms[lo];
-        const long long t = (vb - d.block_start[which]) * BLOCK + threadIdx.x;
-        const Cells c = cells_of_index<CPT>(d.g, t);
+    constexpr int kChunks = (int)(sizeof(BatchDomain) / 16);
+    static_assert(kChunks <= BLOCK, "one thread per descriptor chunk");
+    __shared__ BatchDomain desc[2];
+    const long long stride = gridDim.x;
+    long long vb = blockIdx.x;
+    if (vb >= vblocks) return;
+    const uint32_t step = step_of<St>(step_base, step_off);
+    if (threadIdx.x < kChunks)
+        cp_async16(reinterpret_cast<uint4*>(&desc[0]) + threadIdx.x,
+                   reinterpret_cast<const uint4*>(doms + vb_dom[vb]) + threadIdx.x);
+    cp_async_commit();
+    int next_dom = vb + stride < vblocks ? vb_dom[vb + stride] : 0;
+    for (int buf = 0; vb < vblocks; vb += stride, buf ^= 1) {
+        cp_async_wait_all();
+        __syncthreads();
+        if (vb + stride < vblocks && threadIdx.x < kChunks)
+            cp_async16(reinterpret_cast<uint4*>(&desc[buf ^ 1]) + threadIdx.x,
+                       reinterpret_cast<const uint4*>(doms + next_dom) + threadIdx.x);
+        cp_async_commit();
+        next_dom = vb + 2 * stride < vblocks ? vb_dom[vb + 2 * stride] : 0;
+        const BatchDomain& d = desc[buf];
+        const Cells c = cells_of_vblock(d, which, (uint32_t)(vb - d.block_start[which]) * BLOCK + threadIdx.x);
         const uint32_t ds = step + d.step0;
         if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
         else if constexpr (kExchange)
@@ -633,8 +682,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
 }
 
 template <class St, int VARIANT, bool kAlpha>
-cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, long long vblocks,
-                                const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_kernel(const BatchArgs& a, cudaStream_t st)
 {
     constexpr FastVariant fv = kFastMenu[VARIANT];
     constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
@@ -646,41 +694,33 @@ cudaError_t launch_batch_kernel(void* pool, const BatchDomain* doms, int ndom, l
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, k.block, 0);
     if (e != cudaSuccess) return e;
     long long grid = (long long)(per_sm > 0 ? per_sm : 1) * sms;
-    if (grid > vblocks) grid = vblocks;
+    if (grid > a.vblocks) grid = a.vblocks;
     if (grid < 1) return cudaSuccess;
-    kern<<<(int)grid, k.block, 0, st>>>(static_cast<typename St::bits*>(pool), doms, ndom, vblocks, step_base,
-                                        step_off);
+    kern<<<(int)grid, k.block, 0, st>>>(static_cast<typename St::bits*>(a.pool), a.doms, a.vb_dom, a.vblocks,
+                                        a.step_base, a.step_off);
     return cudaGetLastError();
 }
 
 template <class St, int VARIANT>
-cudaError_t launch_batch_variant(bool alpha, void* pool, const BatchDomain* doms, int ndom, long long vblocks,
-                                 const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_variant(bool alpha, const BatchArgs& a, cudaStream_t st)
 {
-    return alpha ? launch_batch_kernel<St, VARIANT, true>(pool, doms, ndom, vblocks, step_base, step_off, st)
-                 : launch_batch_kernel<St, VARIANT, false>(pool, doms, ndom, vblocks, step_base, step_off, st);
+    return alpha ? launch_batch_kernel<St, VARIANT, true>(a, st) : launch_batch_kernel<St, VARIANT, false>(a, st);
 }
 
 template <class St, size_t... I>
-cudaError_t launch_batch_table(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st,
-                               std::index_sequence<I...>)
+cudaError_t launch_batch_table(int variant, bool alpha, const BatchArgs& a, cudaStream_t st, std::index_sequence<I...>)
 {
-    using Fn = cudaError_t (*)(bool, void*, const BatchDomain*, int, long long, const uint32_t*, uint32_t,
-                               cudaStream_t);
+    using Fn = cudaError_t (*)(bool, const BatchArgs&, cudaStream_t);
     static constexpr Fn table[] = {&launch_batch_variant<St, (int)I>...};
-    return table[variant](alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    return table[variant](alpha, a, st);
 }
 
-// `vblocks`: the virtual blocks of the kernel launched (alpha or beta shape).
 // The step of domain d is *step_base + step_off + d.step0.
 template <class St>
-cudaError_t launch_batch_menu(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_menu(int variant, bool alpha, const BatchArgs& a, cudaStream_t st)
 {
     if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
-    return launch_batch_table<St>(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st,
-                                  std::make_index_sequence<kRegisterVariants>{});
+    return launch_batch_table<St>(variant, alpha, a, st, std::make_index_sequence<kRegisterVariants>{});
 }
 
 }  // namespace lbm

@@ -8,6 +8,7 @@
 #include <utility>
 
 #include "lbm_core.cuh"
+#include "lbm_fast.cuh"
 #include "lbm_kernels.h"
 
 namespace lbm {
@@ -415,19 +416,46 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, 
     block = k.block;
 }
 
-cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st)
+cudaError_t launch_batch_step(int storage, int variant, bool alpha, const BatchArgs& a, cudaStream_t st)
 {
     if (variant < 0 || variant >= kRegisterVariants) return cudaErrorInvalidValue;
     count_launch();
     switch (storage) {
-    case 0: return launch_batch_f64(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
-    case 1: return launch_batch_f32(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
-    case 2: return launch_batch_f16s(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
-    case 3: return launch_batch_bf16s(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
-    case 4: return launch_batch_f16sr(variant, alpha, pool, doms, ndom, vblocks, step_base, step_off, st);
+    case 0: return launch_batch_f64(variant, alpha, a, st);
+    case 1: return launch_batch_f32(variant, alpha, a, st);
+    case 2: return launch_batch_f16s(variant, alpha, a, st);
+    case 3: return launch_batch_bf16s(variant, alpha, a, st);
+    case 4: return launch_batch_f16sr(variant, alpha, a, st);
     default: return cudaErrorInvalidValue;
     }
+}
+
+// Domain of every virtual block of kernel `which` (vb_dom[vb]), by binary
+// search of the table's block_start; rebuilt whenever the table changes.
+__global__ void __launch_bounds__(256) batch_map(const BatchDomain* __restrict__ doms, const int ndom,
+                                                 const long long vblocks, const int which, int* __restrict__ vb_dom)
+{
+    for (long long vb = (long long)blockIdx.x * blockDim.x + threadIdx.x; vb < vblocks;
+         vb += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = ndom - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (doms[mid].block_start[which] <= vb) lo = mid;
+            else hi = mid - 1;
+        }
+        vb_dom[vb] = lo;
+    }
+}
+
+cudaError_t launch_batch_map(const BatchDomain* doms, int ndom, long long vblocks, int which, int* vb_dom,
+                             cudaStream_t st)
+{
+    if (vblocks <= 0 || ndom <= 0) return cudaSuccess;
+    const long long want = (vblocks + 255) / 256;
+    const int grid = (int)(want < 4096 ? want : 4096);
+    count_launch();
+    batch_map<<<grid, 256, 0, st>>>(doms, ndom, vblocks, which, vb_dom);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,

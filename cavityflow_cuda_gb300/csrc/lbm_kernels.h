@@ -92,18 +92,23 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cells
 
 // Batches of box cavities (lbm_fast.cuh): register variants only.
 struct BatchDomain;
-cudaError_t launch_batch_step(int storage, int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
-cudaError_t launch_batch_f64(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                             long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
-cudaError_t launch_batch_f32(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                             long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
-cudaError_t launch_batch_f16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                              long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
-cudaError_t launch_batch_f16sr(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
-cudaError_t launch_batch_bf16s(int variant, bool alpha, void* pool, const BatchDomain* doms, int ndom,
-                               long long vblocks, const uint32_t* step_base, uint32_t step_off, cudaStream_t st);
+struct BatchArgs {
+    void* pool;               // the domains' populations
+    const BatchDomain* doms;  // packed table
+    const int* vb_dom;        // domain of each virtual block of the launched kernel
+    long long vblocks;        // virtual blocks of the launched kernel (alpha or beta shape)
+    const uint32_t* step_base;
+    uint32_t step_off;        // domain d's step: *step_base + step_off + d.step0
+};
+cudaError_t launch_batch_step(int storage, int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+cudaError_t launch_batch_f64(int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+cudaError_t launch_batch_f32(int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+cudaError_t launch_batch_f16s(int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+cudaError_t launch_batch_f16sr(int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+cudaError_t launch_batch_bf16s(int variant, bool alpha, const BatchArgs& a, cudaStream_t st);
+// Rebuilds vb_dom for kernel `which` (0 alpha, 1 beta) from the table.
+cudaError_t launch_batch_map(const BatchDomain* doms, int ndom, long long vblocks, int which, int* vb_dom,
+                             cudaStream_t st);
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,

@@ -122,6 +122,8 @@ struct lbm_server {
     std::vector<lbm::BatchDomain> table;
     lbm::BatchDomain* dtable = nullptr;
     size_t dtable_cap = 0;
+    int* vb_map[2] = {nullptr, nullptr};  // domain of each virtual block, per kernel
+    long long vb_cap[2] = {0, 0};
     uint32_t* zero_word = nullptr;  // step base of the round launches (a request's step is its own count)
     cudaStream_t stream = nullptr;
     int64_t next_id = 1;
@@ -231,9 +233,10 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&v
         for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
             int cpt = 1, block = 1;
             lbm::fast_variant_shape(s->cfg.storage, s->variant, kind == 0, d.g.nx, cpt, block);
-            const long long groups = (long long)((d.g.nx + cpt - 1) / cpt) * d.g.ny * d.g.nz;
+            const long long n = lbm::set_batch_shape(d, kind, cpt, block);
+            if (n < 0) return fail(LBM_ERR_INVALID_ARGUMENT, "request %lld is too large", (long long)reqs[i]->id);
             d.block_start[kind] = next[kind];
-            next[kind] += (groups + block - 1) / block;
+            next[kind] += n;
         }
     }
     vblocks[0] = next[0];
@@ -248,6 +251,19 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&v
     CK(cudaMemcpyAsync(s->dtable, s->table.data(), reqs.size() * sizeof(lbm::BatchDomain), cudaMemcpyHostToDevice,
                        s->stream),
        "cudaMemcpyAsync server table");
+    for (int kind = 0; kind < 2; ++kind) {
+        if (vblocks[kind] > s->vb_cap[kind]) {
+            CK(cudaStreamSynchronize(s->stream), "server block map");
+            if (s->vb_map[kind]) cudaFree(s->vb_map[kind]);
+            s->vb_map[kind] = nullptr;
+            s->vb_cap[kind] = 0;
+            const long long cap = std::max<long long>(vblocks[kind] + vblocks[kind] / 2, 1024);
+            CK(cudaMalloc(&s->vb_map[kind], (size_t)cap * sizeof(int)), "cudaMalloc server block map");
+            s->vb_cap[kind] = cap;
+        }
+        CK(lbm::launch_batch_map(s->dtable, (int)reqs.size(), vblocks[kind], kind, s->vb_map[kind], s->stream),
+           "server block map");
+    }
     return LBM_OK;
 }
 
@@ -330,6 +346,8 @@ int lbm_server_destroy(lbm_server* s)
     for (Request* r : s->queue) delete r;
     for (auto& kv : s->finished) delete kv.second;
     if (s->dtable) cudaFree(s->dtable);
+    for (int kind = 0; kind < 2; ++kind)
+        if (s->vb_map[kind]) cudaFree(s->vb_map[kind]);
     if (s->zero_word) cudaFree(s->zero_word);
     if (s->arena) cudaFree(s->arena);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -404,10 +422,11 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     long long vblocks[2] = {0, 0};
     if (int rc = upload_table(s, run, vblocks)) return rc;
     const auto t_start = std::chrono::steady_clock::now();
-    for (int64_t i = 0; i < q; ++i)
-        CK(lbm::launch_batch_step(s->cfg.storage, s->variant, (i & 1) == 0, s->arena, s->dtable, (int)run.size(),
-                                  vblocks[i & 1], s->zero_word, (uint32_t)i, s->stream),
-           "server step launch");
+    for (int64_t i = 0; i < q; ++i) {
+        const int kind = (int)(i & 1);
+        const lbm::BatchArgs a{s->arena, s->dtable, s->vb_map[kind], vblocks[kind], s->zero_word, (uint32_t)i};
+        CK(lbm::launch_batch_step(s->cfg.storage, s->variant, kind == 0, a, s->stream), "server step launch");
+    }
     CK(cudaStreamSynchronize(s->stream), "server round");
     const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     s->busy_s += dt;
