@@ -8,6 +8,8 @@ MLUPS counts interior cells x steps (src/CController.cpp:1463-1464).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                     [--storage f32|f64|f16s|bf16s|f16sr] [--size 384]
+    python bench.py --workload batch|serve|precision [--batch-storages f32,f16s,f16sr]
+                    [--batch-variant V] [--batch-count 512] [--batch-steps 2000]
 
 Prints ONE JSON line (rank 0).  Keys beyond the base contract:
   roofline      -- dominant kernel's algorithmic bytes / CUDA-event time vs
@@ -62,6 +64,9 @@ def parse():
     ap.add_argument("--no-extensions", action="store_true", help="skip the bounded extension measurements")
     ap.add_argument("--batch-count", type=int, default=512)
     ap.add_argument("--batch-steps", type=int, default=2000)
+    ap.add_argument("--batch-storages", default="f32,f16s,f16sr", help="storages of --workload batch / serve")
+    ap.add_argument("--batch-variant", type=int, default=-1,
+                    help="register variant of --workload batch (default: autotuned per storage)")
     ap.add_argument("--precision-size", type=int, default=512)
     ap.add_argument("--precision-steps", type=int, default=5000)
     ap.add_argument("--serve-count", type=int, default=1000)
@@ -261,7 +266,7 @@ def profile_traffic(a, kernel):
     return e["dram_bytes_per_launch"] * (a.size ** 3) / float(e["cells"])
 
 
-def batch_measure(storage, count, steps, device=0, autotune=True):
+def batch_measure(storage, count, steps, device=0, variant=-1):
     """Aggregate MLUPS of the seeded batch of box cavities (512 edges in
     [16,96], lid in [0.02,0.1], Re log-uniform in [10,2000], seed 0), all
     advanced together; CUDA events around `steps` steps on one stream."""
@@ -273,7 +278,11 @@ def batch_measure(storage, count, steps, device=0, autotune=True):
     cav = batch_workload(count=count, seed=0)
     stream = torch.cuda.Stream()
     with LbmBatch([c.solver_args(storage) for c in cav], storage=storage, device=device) as b:
-        tuned = b.autotune(pairs=3) if autotune else (b.info()["fast_variant"], [])
+        if variant < 0:
+            tuned = b.autotune(pairs=3)
+        else:
+            b.set_fast_variant(variant)
+            tuned = (variant, [])
         b.run(4, stream=stream)
         stream.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -429,8 +438,9 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        res = {s: batch_measure(s, a.batch_count, a.batch_steps) for s in ("f32", "f16s", "f16sr")}
-        for s in ("f32", "f16s", "f16sr"):
+        storages = a.batch_storages.split(",")
+        res = {s: batch_measure(s, a.batch_count, a.batch_steps, variant=a.batch_variant) for s in storages}
+        for s in storages:
             res[s]["single_domain_384_mlups"] = round(single_measure(s, 384, 400), 1)
             res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s]["single_domain_384_mlups"], 3)
         print(json.dumps({"workload": "batch", "results": res}), flush=True)
@@ -439,7 +449,7 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        res = {s_: serve_measure(s_, a.serve_count, a.serve_step_scale) for s_ in ("f32", "f16s", "f16sr")}
+        res = {s_: serve_measure(s_, a.serve_count, a.serve_step_scale) for s_ in a.batch_storages.split(",")}
         print(json.dumps({"workload": "serve", "results": res}), flush=True)
         return
     if a.workload == "precision":
