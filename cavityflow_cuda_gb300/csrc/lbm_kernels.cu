@@ -288,20 +288,24 @@ __global__ void reduce_final(const double* __restrict__ partials, int nblocks, d
     }
 }
 
-// Cuboid of one slot <-> packed host-type buffer, unshifting (f = s + w) on
-// the way out and shifting on the way in for 16-bit storage.
+// Cuboid of one slot <-> packed float buffer (x fastest), unshifting (f = s +
+// w) on the way out and shifting on the way in for 16-bit storage.  A block
+// walks whole rows (one division per row), its threads along x, so both sides
+// are coalesced.
 template <class St>
 __global__ void pack_slot(const typename St::bits* __restrict__ dd, const Grid g, int k, const int3 o,
                           const int3 s, float* __restrict__ out)
 {
-    const long long n = (long long)s.x * s.y * s.z;
+    const long long rows = (long long)s.y * s.z;
     const float w = weight<float>(k);
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int x = o.x + (int)(t % s.x), y = o.y + (int)((t / s.x) % s.y);
-        const int z = o.z + (int)(t / ((long long)s.x * s.y));
-        const float v = St::load(dd[k * g.S + g.idx(x, y, z)]);
-        out[t] = St::shifted ? v + w : v;
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int y = o.y + (int)(r % s.y), z = o.z + (int)(r / s.y);
+        const typename St::bits* src = dd + k * g.S + g.idx(o.x, y, z);
+        float* dst = out + r * s.x;
+        for (int x = threadIdx.x; x < s.x; x += blockDim.x) {
+            const float v = St::load(src[x]);
+            dst[x] = St::shifted ? v + w : v;
+        }
     }
 }
 
@@ -309,14 +313,16 @@ template <class St>
 __global__ void unpack_slot(typename St::bits* __restrict__ dd, const Grid g, int k, const int3 o,
                             const int3 s, const float* __restrict__ in)
 {
-    const long long n = (long long)s.x * s.y * s.z;
+    const long long rows = (long long)s.y * s.z;
     const float w = weight<float>(k);
-    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int x = o.x + (int)(t % s.x), y = o.y + (int)((t / s.x) % s.y);
-        const int z = o.z + (int)(t / ((long long)s.x * s.y));
-        const float v = in[t];
-        dd[k * g.S + g.idx(x, y, z)] = St::store(St::shifted ? v - w : v);
+    for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+        const int y = o.y + (int)(r % s.y), z = o.z + (int)(r / s.y);
+        typename St::bits* dst = dd + k * g.S + g.idx(o.x, y, z);
+        const float* src = in + r * s.x;
+        for (int x = threadIdx.x; x < s.x; x += blockDim.x) {
+            const float v = src[x];
+            dst[x] = St::store(St::shifted ? v - w : v);
+        }
     }
 }
 
@@ -540,12 +546,12 @@ cudaError_t launch_reduce(int storage, const void* dd, const uint8_t* flags, con
 cudaError_t launch_pack_slot(int storage, const void* dd, const Grid& g, int k, int3 o, int3 s, float* out,
                              cudaStream_t st)
 {
-    const long long n = (long long)s.x * s.y * s.z;
+    const long long rows = (long long)s.y * s.z;
     count_launch();
     return with_storage(storage, [&](auto tag) {
         using St = decltype(tag);
-        pack_slot<St><<<grid_for(n, 256, 8192), 256, 0, st>>>(static_cast<const typename St::bits*>(dd), g, k,
-                                                               o, s, out);
+        pack_slot<St><<<grid_for(rows, 1, 65536), 256, 0, st>>>(static_cast<const typename St::bits*>(dd), g, k,
+                                                                 o, s, out);
         return cudaGetLastError();
     });
 }
@@ -553,12 +559,12 @@ cudaError_t launch_pack_slot(int storage, const void* dd, const Grid& g, int k, 
 cudaError_t launch_unpack_slot(int storage, void* dd, const Grid& g, int k, int3 o, int3 s, const float* in,
                                cudaStream_t st)
 {
-    const long long n = (long long)s.x * s.y * s.z;
+    const long long rows = (long long)s.y * s.z;
     count_launch();
     return with_storage(storage, [&](auto tag) {
         using St = decltype(tag);
-        unpack_slot<St><<<grid_for(n, 256, 8192), 256, 0, st>>>(static_cast<typename St::bits*>(dd), g, k, o, s,
-                                                                 in);
+        unpack_slot<St><<<grid_for(rows, 1, 65536), 256, 0, st>>>(static_cast<typename St::bits*>(dd), g, k, o,
+                                                                   s, in);
         return cudaGetLastError();
     });
 }
