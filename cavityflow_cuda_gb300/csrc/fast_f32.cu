@@ -1,9 +1,8 @@
 // fast_f32.cu -- instantiates the vectorised and the row-pipelined (bulk copy)
-// step kernels, the fused-pair kernels and the batch kernels for F32 storage
-// (one translation unit per storage type, so they compile in parallel).
+// step kernels and the batch kernels for F32 storage (one translation unit per
+// storage type, so they compile in parallel).
 #include "lbm_fast.cuh"
 #include "lbm_kernels.h"
-#include "lbm_pair.cuh"
 #include "lbm_tma.cuh"
 
 namespace lbm {
@@ -23,12 +22,6 @@ cudaError_t launch_tma_f32(bool alpha, void* dd, const Grid& g, const Params& p,
 cudaError_t launch_batch_f32(int variant, bool alpha, const BatchArgs& a, cudaStream_t st)
 {
     return launch_batch_menu<F32>(variant, alpha, a, st);
-}
-
-cudaError_t launch_pair_f32(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
-                            cudaStream_t st)
-{
-    return launch_pair_menu<F32>(pv, dd, g, p, lid_y, sync, err, st);
 }
 
 }  // namespace lbm

@@ -132,8 +132,7 @@ int lbm_detail::check_kernel_flag(lbm_solver* s)
     CK(cudaMemcpy(&flag, err_flag(s), sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy error flag");
     if (flag) {
         CK(cudaMemset(err_flag(s), 0, sizeof(int)), "cudaMemset error flag");
-        return fail(LBM_ERR_TIMEOUT,
-                    "a step kernel gave up waiting (flag %d: 1, 2 bulk copies; 4 a fused pair's alpha planes)", flag);
+        return fail(LBM_ERR_TIMEOUT, "a step kernel gave up waiting for its bulk copies (flag %d)", flag);
     }
     return LBM_OK;
 }
@@ -279,16 +278,6 @@ cudaError_t copy_slot(lbm_solver* s, int k, int3 o, int3 n, void* host, bool to_
     }
     m.extent = make_cudaExtent((size_t)n.x * elem, (size_t)n.y, (size_t)n.z);
     return cudaMemcpy3DAsync(&m, st);
-}
-
-// Device scratch of the fused-pair launches (allocated on first use).
-int ensure_pair_sync(lbm_solver* s)
-{
-    if (s->pair_sync) return LBM_OK;
-    const size_t bytes = (size_t)(s->g.nz + 1) * sizeof(uint32_t);
-    CK(cudaMalloc(&s->pair_sync, bytes), "cudaMalloc pair counters");
-    s->device_bytes += (int64_t)bytes;
-    return LBM_OK;
 }
 
 int ensure_staging(lbm_solver* s, size_t elems)
@@ -518,7 +507,6 @@ void lbm_detail::destroy_solver(lbm_solver* s)
     if (s->scratch) cudaFree(s->scratch);
     if (s->counts) cudaFree(s->counts);
     if (s->staging) cudaFree(s->staging);
-    if (s->pair_sync) cudaFree(s->pair_sync);
     if (s->host_out) cudaFreeHost(s->host_out);
     delete s;
 }
@@ -550,8 +538,8 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     lbm::fast_variant_shape(s->storage, s->variant, true, s->g.nx, info->cells_per_thread, info->block_threads);
     lbm::fast_variant_shape(s->storage, s->variant, false, s->g.nx, info->beta_cells_per_thread,
                             info->beta_block_threads);
-    const int sv = lbm::step_variant(s->variant);
-    info->beta_block_exchange = sv < lbm::kRegisterVariants && lbm::kFastMenu[sv].block_exchange ? 1 : 0;
+    info->beta_block_exchange =
+        s->variant < lbm::kRegisterVariants && lbm::kFastMenu[s->variant].block_exchange ? 1 : 0;
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
@@ -619,10 +607,6 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
         if (int r = step(s, false, nullptr, nullptr, st)) return r;
         --left;
     }
-    // pair variants run each alpha/beta pair as one fused launch
-    const bool pair = s->lid_y >= 0 && lbm::is_pair_variant(s->variant);
-    if (pair)
-        if (int r = ensure_pair_sync(s)) return r;
     const int64_t per_graph = 2 * kGraphPairs;
     if (s->lid_y >= 0 && left >= per_graph) {
         if (!s->graph) {
@@ -635,11 +619,6 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             p.step_base = step_words(s);
             for (int i = 0; i < kGraphPairs && e == cudaSuccess; ++i) {
                 p.step_off = (uint32_t)(2 * i);
-                if (pair) {
-                    e = lbm::launch_pair_step(s->storage, s->variant, s->dd, s->g, p, s->lid_y, s->pair_sync,
-                                              err_flag(s), s->capture_stream);
-                    continue;
-                }
                 e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, p, s->lid_y, err_flag(s),
                                           s->capture_stream);
                 p.step_off = (uint32_t)(2 * i + 1);
@@ -663,23 +642,12 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             if (lbm::storage_stochastic(s->storage))
                 CK(lbm::launch_set_step(step_words(s), (uint32_t)s->counter, st), "step word launch");
             CK(cudaGraphLaunch(s->graph, st), "cudaGraphLaunch");
-            lbm::add_launches(pair ? kGraphPairs : per_graph);
+            lbm::add_launches(per_graph);
             s->counter += per_graph;
             left -= per_graph;
         }
         s->last_alpha = false;
         s->macros_fresh = false;
-    }
-    while (pair && left >= 2) {
-        lbm::Params p = s->p;
-        p.step_base = step_words(s) + 1;
-        p.step_off = (uint32_t)s->counter;
-        CK(lbm::launch_pair_step(s->storage, s->variant, s->dd, s->g, p, s->lid_y, s->pair_sync, err_flag(s), st),
-           "pair step launch");
-        s->counter += 2;
-        s->last_alpha = false;
-        s->macros_fresh = false;
-        left -= 2;
     }
     while (left > 0) {
         if (int r = step(s, !s->last_alpha, nullptr, nullptr, st)) return r;
@@ -719,7 +687,6 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     if (s->lid_y < 0) return fail(LBM_ERR_UNSUPPORTED, "autotune needs the vectorised (box cavity) path");
     CK(cudaSetDevice(s->device), "cudaSetDevice");
     CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
-    if (int r = ensure_pair_sync(s)) return r;
     const size_t bytes = (size_t)lbm::Q * s->g.S * elem_bytes(s->storage);
     void* saved = nullptr;
     CK(cudaMalloc(&saved, bytes), "cudaMalloc autotune snapshot");
@@ -730,12 +697,6 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     int best_v = s->variant;
     auto run_pairs = [&](int v, int n) -> cudaError_t {
         for (int i = 0; i < n; ++i) {
-            if (lbm::is_pair_variant(v)) {
-                cudaError_t e = lbm::launch_pair_step(s->storage, v, s->dd, s->g, s->p, s->lid_y, s->pair_sync,
-                                                      err_flag(s), st);
-                if (e != cudaSuccess) return e;
-                continue;
-            }
             cudaError_t e = lbm::launch_fast_step(s->storage, v, true, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
             if (e == cudaSuccess)
                 e = lbm::launch_fast_step(s->storage, v, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);

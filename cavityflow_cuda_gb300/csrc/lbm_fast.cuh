@@ -49,16 +49,6 @@ template <> struct RawVec<8> { using type = uint2; };
 template <> struct RawVec<4> { using type = unsigned int; };
 template <> struct RawVec<2> { using type = unsigned short; };
 
-// A global load, optionally cached in L2 only (CG): a fused alpha+beta launch
-// reads in beta what other SMs wrote in alpha during the same launch, which a
-// stale L1 line could hide.
-template <bool CG, class R>
-__device__ __forceinline__ R load_from(const R* p)
-{
-    if constexpr (CG) return __ldcg(p);
-    else return *p;
-}
-
 // Aligned access to N consecutive storage elements, converted to the
 // arithmetic type.
 template <class St, int N>
@@ -86,11 +76,10 @@ struct Vio {
     }
     // Storage-typed access: 16-bit populations stay packed in registers and
     // are converted one cell at a time, which halves their register footprint.
-    template <bool CG = false>
     __device__ static void load_raw(const bits* p, bits (&a)[N])
     {
         Pack x;
-        x.u = load_from<CG>(reinterpret_cast<const raw*>(p));
+        x.u = *reinterpret_cast<const raw*>(p);
 #pragma unroll
         for (int v = 0; v < N; ++v) a[v] = x.b[v];
     }
@@ -218,7 +207,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
 // Beta step of the CPT cells of group `c`.  All 32 lanes of the warp must
 // call it together, with consecutive groups (they exchange edge elements by
 // shuffles); lanes past the domain's end take part in the shuffles only.
-template <class St, int CPT, bool CG = false>
+template <class St, int CPT>
 __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                            const typename St::T inv_tau, const typename St::T lid_u,
                                            const int lid_y, const Cells c, const uint32_t step)
@@ -248,7 +237,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
         constexpr int cx = dir_x(k);
         const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
         bits a[CPT];
-        if (active) IO::template load_raw<CG>(dd + rb, a);
+        if (active) IO::load_raw(dd + rb, a);
         else {
 #pragma unroll
             for (int v = 0; v < CPT; ++v) a[v] = bits(0);
@@ -259,14 +248,14 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
             edge[k] = bits(0);
         } else if constexpr (cx == 1) {
             bits nb = shfl_down_bits(a[0], 1);
-            if (active && !right_in) nb = load_from<CG>(dd + rb + CPT);
+            if (active && !right_in) nb = dd[rb + CPT];
 #pragma unroll
             for (int v = 0; v < CPT - 1; ++v) p[k][v] = a[v + 1];
             p[k][CPT - 1] = nb;
             edge[k] = a[0];
         } else {
             bits pb = shfl_up_bits(a[CPT - 1], 1);
-            if (active && !left_in) pb = load_from<CG>(dd + rb - 1);
+            if (active && !left_in) pb = dd[rb - 1];
             p[k][0] = pb;
 #pragma unroll
             for (int v = 1; v < CPT; ++v) p[k][v] = a[v - 1];
@@ -339,7 +328,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
 // odd element with a scalar access; every other thread issues exactly 19
 // vector loads and 19 vector stores, as in alpha.  All BLOCK threads of the
 // block must call it together, with consecutive groups.
-template <class St, int CPT, int BLOCK, bool CG = false>
+template <class St, int CPT, int BLOCK>
 __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ dd, const Grid& g,
                                                const typename St::T inv_tau, const typename St::T lid_u,
                                                const int lid_y, const Cells c, const uint32_t step)
@@ -369,12 +358,12 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
         constexpr int k = decltype(kc)::value;
         constexpr int cx = dir_x(k);
         const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
-        IO::template load_raw<CG>(dd + rb, a[k]);
+        IO::load_raw(dd + rb, a[k]);
         ext[k] = bits(0);
         if constexpr (cx == 1) {
-            if (active && !right_in) ext[k] = load_from<CG>(dd + rb + CPT);
+            if (active && !right_in) ext[k] = dd[rb + CPT];
         } else if constexpr (cx == -1) {
-            if (active && !left_in) ext[k] = load_from<CG>(dd + rb - 1);
+            if (active && !left_in) ext[k] = dd[rb - 1];
         }
     });
     // warp-edge lanes publish the elements the neighbouring warps need

@@ -25,7 +25,6 @@ struct lbm_solver {
                                            // step words [4] (see step_words)
     double* host_out = nullptr;     // pinned, 4 doubles
     float* staging = nullptr;       // 16-bit storage: one packed slot cuboid
-    uint32_t* pair_sync = nullptr;  // fused-pair launches: ticket + per-plane counters (nz + 1 words)
     size_t staging_elems = 0;
     int64_t counter = 0;
     bool last_alpha = false;

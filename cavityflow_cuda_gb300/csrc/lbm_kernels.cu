@@ -397,7 +397,7 @@ cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned lo
 bool fast_variant_fits(int storage, int variant, const Grid& g)
 {
     if (variant < 0 || variant >= kFastVariantCount) return false;
-    if (variant < kRegisterVariants || is_pair_variant(variant)) return true;
+    if (variant < kRegisterVariants) return true;
     const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
     const int elem = storage == 0 ? 8 : storage == 1 ? 4 : 2;
     int dev = 0, max_optin = 0;
@@ -410,7 +410,6 @@ bool fast_variant_fits(int storage, int variant, const Grid& g)
 
 void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, int& block)
 {
-    variant = step_variant(variant);
     if (variant >= kRegisterVariants) {
         const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
         block = 32 * (1 + c.consumer_warps);
@@ -468,8 +467,7 @@ cudaError_t launch_batch_map(const BatchDomain* doms, int ndom, long long vblock
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
                              int lid_y, int* err, cudaStream_t st)
 {
-    variant = step_variant(variant);
-    if (variant >= kRegisterVariants && variant < kFirstPairVariant) {
+    if (variant >= kRegisterVariants && variant < kFastVariantCount) {
         const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
         cudaError_t e;
         switch (storage) {
@@ -490,22 +488,6 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
     case 2: return launch_fast_f16s(variant, alpha, dd, g, p, lid_y, st);
     case 3: return launch_fast_bf16s(variant, alpha, dd, g, p, lid_y, st);
     case 4: return launch_fast_f16sr(variant, alpha, dd, g, p, lid_y, st);
-    default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_pair_step(int storage, int variant, void* dd, const Grid& g, const Params& p, int lid_y,
-                             uint32_t* sync, int* err, cudaStream_t st)
-{
-    if (!is_pair_variant(variant)) return cudaErrorInvalidValue;
-    const int pv = variant - kFirstPairVariant;
-    count_launch();
-    switch (storage) {
-    case 0: return launch_pair_f64(pv, dd, g, p, lid_y, sync, err, st);
-    case 1: return launch_pair_f32(pv, dd, g, p, lid_y, sync, err, st);
-    case 2: return launch_pair_f16s(pv, dd, g, p, lid_y, sync, err, st);
-    case 3: return launch_pair_bf16s(pv, dd, g, p, lid_y, sync, err, st);
-    case 4: return launch_pair_f16sr(pv, dd, g, p, lid_y, sync, err, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -81,34 +81,9 @@ constexpr int kTmaVariants = 6;
 constexpr TmaConfig kTmaMenu[kTmaVariants] = {
     {1, 3, 6}, {1, 4, 6}, {2, 2, 8}, {2, 3, 8}, {1, 2, 4}, {4, 2, 8},
 };
-// Fused pair variants (lbm_pair.cuh): one launch runs an alpha step and the
-// beta step after it.  base: the register variant whose shape both halves use
-// (its alpha and beta shapes are equal; single steps run its kernels);
-// window_mb: the L2 working set the plane lookahead is sized to;
-// items_per_ticket: thread blocks' worth of cells a CTA takes at a time.
-struct PairConfig {
-    int base;
-    int window_mb;
-    int items_per_ticket;
-};
-constexpr int kPairVariants = 10;
-constexpr PairConfig kPairMenu[kPairVariants] = {
-    {9, 64, 1}, {9, 64, 2}, {9, 64, 4}, {9, 64, 8}, {9, 96, 4}, {9, 32, 4}, {8, 64, 4}, {8, 64, 8}, {11, 64, 2}, {11, 64, 4},
-};
-constexpr int kFirstPairVariant = kRegisterVariants + kTmaVariants;
-constexpr int kFastVariantCount = kFirstPairVariant + kPairVariants;
-constexpr bool is_pair_variant(int variant) { return variant >= kFirstPairVariant && variant < kFastVariantCount; }
-// The variant whose kernels run single steps (a pair variant's base).
-constexpr int step_variant(int variant)
-{
-    return is_pair_variant(variant) ? kPairMenu[variant - kFirstPairVariant].base : variant;
-}
+constexpr int kFastVariantCount = kRegisterVariants + kTmaVariants;
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
                              int lid_y, int* err, cudaStream_t st);
-// An alpha step and the following beta step in one launch (pair variants);
-// `sync` holds nz + 1 words of device scratch.
-cudaError_t launch_pair_step(int storage, int variant, void* dd, const Grid& g, const Params& p, int lid_y,
-                             uint32_t* sync, int* err, cudaStream_t st);
 // Whether a variant fits this domain (shared memory of the bulk-copy kernels).
 bool fast_variant_fits(int storage, int variant, const Grid& g);
 // Cells per thread and threads per block of a variant's alpha or beta kernel
@@ -143,16 +118,6 @@ cudaError_t launch_fast_f16s(int variant, bool alpha, void* dd, const Grid& g, c
 cudaError_t launch_fast_bf16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                               cudaStream_t st);
 cudaError_t launch_fast_f16sr(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
-                              cudaStream_t st);
-cudaError_t launch_pair_f64(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
-                            cudaStream_t st);
-cudaError_t launch_pair_f32(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
-                            cudaStream_t st);
-cudaError_t launch_pair_f16s(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
-                             cudaStream_t st);
-cudaError_t launch_pair_f16sr(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
-                              cudaStream_t st);
-cudaError_t launch_pair_bf16s(int pv, void* dd, const Grid& g, const Params& p, int lid_y, uint32_t* sync, int* err,
                               cudaStream_t st);
 cudaError_t launch_tma_f64(bool alpha, void* dd, const Grid& g, const Params& p, int lid_y, int rows, int stages,
                            int consumer_warps, int* err, cudaStream_t st);

@@ -259,11 +259,8 @@ int lbm_synchronize(lbm_solver* solver);
 /* Number of launch variants of the box-cavity kernels: 13 register-blocked
  * vector kernels (0..12: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
- * elements per warp or per block), 6 row-pipelined bulk-copy kernels
- * (13..18: rows per unit, buffers, consumer warps) and 10 fused-pair kernels
- * (19..28: lbm_run advances each alpha/beta pair in one launch, beta reading
- * alpha's output from L2; a register shape and an L2 working set; single
- * steps run that shape's register kernels). */
+ * elements per warp or per block) and 6 row-pipelined bulk-copy kernels
+ * (13..18: rows per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Number of register variants (the first variants; the batch kernel's menu). */
 int lbm_register_variant_count(void);

@@ -114,7 +114,7 @@ def test_cli_usage_and_argument_errors(lib, tmp_path):
 
 
 def test_launch_variant_menu_size(lib):
-    """13 register variants (0-12), 6 bulk-copy variants (13-18) and 10
-    fused-pair variants (19-28); the GPU parity tests enumerate exactly these."""
-    assert lib.lbm_fast_variant_count() == 29
+    """13 register variants (0-12) and 6 bulk-copy variants (13-18); the GPU
+    parity tests enumerate exactly these."""
+    assert lib.lbm_fast_variant_count() == 19
     assert lib.lbm_register_variant_count() == 13

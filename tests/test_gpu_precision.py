@@ -19,7 +19,7 @@ def shifted_solver(n, storage, inv_tau, lid, **kw):
 
 
 @pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
-@pytest.mark.parametrize("variant", range(29))
+@pytest.mark.parametrize("variant", range(19))
 def test_shifted_storage_matches_oracle(gpu, oracle, storage, variant):
     _, itau = orc.tau_of(0.0192, np.float32)
     lid = np.float32(0.08)
@@ -40,23 +40,6 @@ def test_shifted_storage_matches_oracle(gpu, oracle, storage, variant):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (storage, variant, n)
         ran += 1
     assert ran >= 2
-
-
-@pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
-@pytest.mark.parametrize("variant", [19, 22, 25, 28])
-def test_shifted_fused_pairs_match_oracle(gpu, oracle, storage, variant):
-    """Fused alpha+beta launches in 16-bit storage on a domain deep enough for
-    the interleaved job order, through graph replays (150 steps); F16SR keys
-    the beta half of each launch with the following step."""
-    _, itau = orc.tau_of(0.0192, np.float32)
-    lid = np.float32(0.08)
-    n, steps = (20, 14, 40), 150
-    dd, _ = oracle.run_cavity_s(*n, KIND[storage], itau, lid, steps)
-    want = oracle.unshift(dd, KIND[storage])
-    with shifted_solver(n, storage, itau, lid, fast_variant=variant) as s:
-        s.run(steps)
-        got = s.get_all()
-    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (storage, variant)
 
 
 def test_stochastic_storage_graph_replays_match_oracle(gpu, oracle):
