@@ -7,7 +7,7 @@ counters, beta on odd, as src/CController.cpp:1278-1287 alternates them);
 MLUPS counts interior cells x steps (src/CController.cpp:1463-1464).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--storage f32|f64|f16s|bf16s|f16sr] [--size 384]
+                    [--storage f32|f64|f16s|bf16s|f16sr] [--size 384] [--variant V]
     python bench.py --workload batch|serve|precision [--batch-storages f32,f16s,f16sr]
                     [--batch-variant V] [--batch-count 512] [--batch-steps 2000]
 
@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--storage", default="f32", choices=list(BYTES_PER_VALUE))
     ap.add_argument("--size", type=int, default=384)
+    ap.add_argument("--variant", type=int, default=-1, help="launch variant (default: the library's for the storage)")
     ap.add_argument("--lid", type=float, default=0.05)
     ap.add_argument("--nu", type=float, default=0.0192)
     ap.add_argument("--no-e2e", action="store_true")
@@ -507,6 +508,8 @@ def run_gpu(a):
 
     with CLbmSolverGB300((n, n, n), lat["inv_tau"], lat["velocity"][0], storage=a.storage, device=local) as s:
         assert s.info()["fast_path"] == 1
+        if a.variant >= 0:
+            s.set_fast_variant(a.variant)
         # warm-up (also captures the run graph)
         s.run(max(a.warmup, 3), stream=stream)
         stream.synchronize()
