@@ -159,6 +159,7 @@ def reference_arm(a):
     lid = dtype(a.lid)
     dd, flags = lib.init(n, n, n, dtype)
     flags[1:-1, n, 1:-1] = orc.VELOCITY_INJECTION
+    gpu_kernels = reference_gpu_kernels(dd, flags, itau, lid, n)
     # per-step sample: a z-slab sized so K+W steps take about two minutes
     probe = (1, 1, 1), (n, n, min(2, n))
     t0 = time.perf_counter()
@@ -184,7 +185,38 @@ def reference_arm(a):
             "cpu_baseline": {"value": round(value, 3), "unit": "MLUPS", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if gpu_kernels is not None:
+        line["gpu_kernels"] = gpu_kernels
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_kernels(dd, flags, itau, lid, n, steps=200, warmup=4):
+    """MLUPS of the reference's own CUDA alpha/beta kernels on this GPU
+    (oracle/ref_gpu.py: src/gpukernels built from source for sm_103a with the
+    reference's nvcc flags, its 32x8x1 blocks), CUDA events over `steps`
+    steps; None where the kernels were not built or no GPU is present."""
+    try:
+        import torch
+
+        from oracle import ref_gpu
+        if not (torch.cuda.is_available() and ref_gpu.available()):
+            return None
+        torch.cuda.set_device(0)
+        stream = torch.cuda.current_stream()
+        with ref_gpu.RefGpuCavity(dd, flags, itau, lid) as ref:
+            ref.run(warmup, stream.cuda_stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ref.run(steps, stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+        return {"value": round(float(n) ** 3 * steps / (ms / 1e3) / 1e6, 1), "unit": "MLUPS", "steps": steps,
+                "what": "the reference's own CUDA alpha/beta kernels (src/gpukernels, built from source for "
+                        "sm_103a with its nvcc flags), 32x8x1 blocks over the domain with its halo, on this GPU"}
+    except Exception as e:  # keep the CPU line whatever happens here
+        return {"error": repr(e)}
 
 
 # ---------------------------------------------------------------------------

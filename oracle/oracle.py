@@ -37,6 +37,7 @@ def build(ref_src: str | None = None) -> None:
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref_src and os.path.isdir(ref_src):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "refgpu", f"REF_SRC={ref_src}"], check=True)
 
 
 def _ptr(a: np.ndarray):
