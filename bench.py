@@ -7,7 +7,7 @@ counters, beta on odd, as src/CController.cpp:1278-1287 alternates them);
 MLUPS counts interior cells x steps (src/CController.cpp:1463-1464).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--storage f32|f64|f16s|bf16s|f16sr] [--size 384] [--variant V]
+                    [--storage f32|f64|f16s|bf16s|f16sr] [--size 384] [--variant V] [--fma]
     python bench.py --workload batch|serve|precision [--batch-storages f32,f16s,f16sr]
                     [--batch-variant V] [--batch-count 512] [--batch-steps 2000]
 
@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--storage", default="f32", choices=list(BYTES_PER_VALUE))
     ap.add_argument("--size", type=int, default=384)
     ap.add_argument("--variant", type=int, default=-1, help="launch variant (default: the library's for the storage)")
+    ap.add_argument("--fma", action="store_true", help="f64: fuse the collision's multiply-adds (not bit-exact)")
     ap.add_argument("--lid", type=float, default=0.05)
     ap.add_argument("--nu", type=float, default=0.0192)
     ap.add_argument("--no-e2e", action="store_true")
@@ -85,7 +86,8 @@ def config_dict(a, world):
             "step": "one lattice time step (alpha/beta alternating), whole domain",
             "l2": f"inputs larger than L2: {19 * (a.size + 2) ** 3 * BYTES_PER_VALUE[a.storage] / 1e9:.2f} GB "
                   f"population array vs {L2_BYTES / 1e6:.0f} MB L2",
-            "parallelism": f"replicas x{world}" if world > 1 else "single domain, 1 GPU"}
+            "parallelism": f"replicas x{world}" if world > 1 else "single domain, 1 GPU",
+            **({"fused_multiply_add": True} if getattr(a, "fma", False) else {})}
 
 
 # ---------------------------------------------------------------------------
@@ -538,7 +540,8 @@ def run_gpu(a):
     if dev_id and not dev_id.startswith("GPU-") and len(dev_id) == 36:
         dev_id = "GPU-" + dev_id
 
-    with CLbmSolverGB300((n, n, n), lat["inv_tau"], lat["velocity"][0], storage=a.storage, device=local) as s:
+    with CLbmSolverGB300((n, n, n), lat["inv_tau"], lat["velocity"][0], storage=a.storage, device=local,
+                         fused_multiply_add=a.fma) as s:
         assert s.info()["fast_path"] == 1
         if a.variant >= 0:
             s.set_fast_variant(a.variant)

@@ -8,7 +8,9 @@ beside it (host/lbm_main.cpp).  Object files go to
 
 The library is compiled with ``-fmad=false``: the FP64/FP32 collision must
 not be contracted into fused multiply-adds, so that it performs the same IEEE
-operations as the reference kernels.
+operations as the reference kernels.  The one exception is ``*_fma.cu``
+(``fast_f64_fma.cu``): the opt-in FP64 kernels whose multiply-adds are fused
+on purpose (lbm_params.fused_multiply_add).
 """
 from __future__ import annotations
 
@@ -63,7 +65,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
             return None
         # .cpp units include the kernel headers, so they are compiled as CUDA too
         lang = ["-x", "cu"] if src.endswith(".cpp") else []
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *lang, "-c", src, "-o", obj]
+        flags = NVCC_FLAGS
+        if src.endswith("_fma.cu"):  # FP64 kernels that fuse multiply-adds on purpose (fast_f64_fma.cu)
+            flags = [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS]
+        cmd = [nvcc, *ARCH, *flags, *lang, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -193,6 +193,13 @@ int refresh_path(lbm_solver* s)
     return LBM_OK;
 }
 
+// Storage code of the vectorised step kernels: FP64 with fused multiply-adds
+// has its own kernel family (lbm::kStorageF64Fma).
+int kernel_storage(const lbm_solver* s)
+{
+    return s->fma && s->storage == LBM_STORAGE_F64 ? lbm::kStorageF64Fma : s->storage;
+}
+
 int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, cudaStream_t st)
 {
     int3 o, n;
@@ -201,7 +208,7 @@ int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, 
     p.step_base = step_words(s) + 1;
     p.step_off = (uint32_t)s->counter;
     if (!origin && s->lid_y >= 0) {
-        e = lbm::launch_fast_step(s->storage, s->variant, alpha, s->dd, s->g, p, s->lid_y, err_flag(s), st);
+        e = lbm::launch_fast_step(kernel_storage(s), s->variant, alpha, s->dd, s->g, p, s->lid_y, err_flag(s), st);
     } else {
         if (origin) {
             int r = resolve_cuboid(s, origin, size, o, n);
@@ -428,6 +435,10 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
     const bool gravity = prm->gravity[0] != 0.0 || prm->gravity[1] != 0.0 || prm->gravity[2] != 0.0;
     if (gravity && prm->storage >= LBM_STORAGE_F16S)
         return fail(LBM_ERR_UNSUPPORTED, "gravity is supported with F64 and F32 storage only");
+    if (prm->fused_multiply_add != 0 && prm->fused_multiply_add != 1)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "fused_multiply_add must be 0 or 1");
+    if (prm->fused_multiply_add && prm->storage != LBM_STORAGE_F64)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "fused_multiply_add applies to F64 storage only");
     if (!(prm->inv_tau > 0) || !std::isfinite(prm->inv_tau) || !std::isfinite(prm->lid_velocity))
         return fail(LBM_ERR_INVALID_ARGUMENT, "inv_tau must be positive and finite");
     int ndev = 0;
@@ -453,6 +464,7 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
                     lbm::kFastVariantCount);
     }
     s->variant = prm->fast_variant == 0 ? default_variant(s->storage) : prm->fast_variant - 1;
+    s->fma = prm->fused_multiply_add == 1;
 
     auto bail = [&](int r) { destroy_solver(s); return r; };
     cudaError_t e = cudaSetDevice(s->device);
@@ -538,6 +550,7 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     lbm::fast_variant_shape(s->storage, s->variant, true, s->g.nx, info->cells_per_thread, info->block_threads);
     lbm::fast_variant_shape(s->storage, s->variant, false, s->g.nx, info->beta_cells_per_thread,
                             info->beta_block_threads);
+    info->fused_multiply_add = s->fma ? 1 : 0;
     info->beta_block_exchange =
         s->variant < lbm::kRegisterVariants && lbm::kFastMenu[s->variant].block_exchange ? 1 : 0;
     info->row_pitch = s->g.P;
@@ -619,11 +632,11 @@ int lbm_run(lbm_solver* s, int64_t steps, void* stream)
             p.step_base = step_words(s);
             for (int i = 0; i < kGraphPairs && e == cudaSuccess; ++i) {
                 p.step_off = (uint32_t)(2 * i);
-                e = lbm::launch_fast_step(s->storage, s->variant, true, s->dd, s->g, p, s->lid_y, err_flag(s),
-                                          s->capture_stream);
+                e = lbm::launch_fast_step(kernel_storage(s), s->variant, true, s->dd, s->g, p, s->lid_y,
+                                          err_flag(s), s->capture_stream);
                 p.step_off = (uint32_t)(2 * i + 1);
                 if (e == cudaSuccess)
-                    e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, p, s->lid_y,
+                    e = lbm::launch_fast_step(kernel_storage(s), s->variant, false, s->dd, s->g, p, s->lid_y,
                                               err_flag(s), s->capture_stream);
             }
             cudaError_t e2 = cudaStreamEndCapture(s->capture_stream, &graph);
@@ -697,9 +710,10 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     int best_v = s->variant;
     auto run_pairs = [&](int v, int n) -> cudaError_t {
         for (int i = 0; i < n; ++i) {
-            cudaError_t e = lbm::launch_fast_step(s->storage, v, true, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+            cudaError_t e =
+                lbm::launch_fast_step(kernel_storage(s), v, true, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
             if (e == cudaSuccess)
-                e = lbm::launch_fast_step(s->storage, v, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+                e = lbm::launch_fast_step(kernel_storage(s), v, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
             if (e != cudaSuccess) return e;
         }
         return cudaSuccess;
@@ -708,7 +722,8 @@ int lbm_autotune(lbm_solver* s, int32_t pairs, int32_t* best, float* ms_per_pair
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (s->last_alpha && e == cudaSuccess)  // the timing runs alpha-first pairs from an even parity
-        e = lbm::launch_fast_step(s->storage, s->variant, false, s->dd, s->g, s->p, s->lid_y, err_flag(s), st);
+        e = lbm::launch_fast_step(kernel_storage(s), s->variant, false, s->dd, s->g, s->p, s->lid_y, err_flag(s),
+                                  st);
     bool any = false;
     for (int v = 0; v < lbm::kFastVariantCount && e == cudaSuccess; ++v) {
         if (!lbm::fast_variant_fits(s->storage, v, s->g)) {

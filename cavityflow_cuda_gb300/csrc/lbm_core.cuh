@@ -116,6 +116,10 @@ struct F64 {
     __device__ static T load_step(bits b) { return load(b); }
     static constexpr int kStepLog2 = 0;
 };
+// FP64 whose step kernels are compiled with fused multiply-adds
+// (fast_f64_fma.cu, the one translation unit built with -fmad=true); a type of
+// its own so that its kernel instantiations never merge with F64's.
+struct F64F : F64 {};
 struct F32 {
     using bits = float;
     using T = float;

@@ -30,6 +30,7 @@ struct lbm_solver {
     bool last_alpha = false;
     int lid_y = -1;                 // fast path: lid row (ny) or 0 for none; -1: flag-array path
     int variant = 0;                // launch variant of the vectorised kernels
+    bool fma = false;               // FP64: fused multiply-adds in the vectorised steps
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int64_t device_bytes = 0;

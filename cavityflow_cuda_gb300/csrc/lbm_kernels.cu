@@ -399,7 +399,7 @@ bool fast_variant_fits(int storage, int variant, const Grid& g)
     if (variant < 0 || variant >= kFastVariantCount) return false;
     if (variant < kRegisterVariants) return true;
     const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
-    const int elem = storage == 0 ? 8 : storage == 1 ? 4 : 2;
+    const int elem = storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 ? 4 : 2;
     int dev = 0, max_optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     if (cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
@@ -417,7 +417,7 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, 
         return;
     }
     const KernelShape k = alpha ? kFastMenu[variant].alpha : kFastMenu[variant].beta;
-    const int V = 16 / (storage == 0 ? 8 : storage == 1 ? 4 : 2);
+    const int V = 16 / (storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 ? 4 : 2);
     cpt = V / k.cpt_div > 0 ? V / k.cpt_div : 1;
     block = k.block;
 }
@@ -471,7 +471,10 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
         const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
         cudaError_t e;
         switch (storage) {
-        case 0: e = launch_tma_f64(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 0:
+        case kStorageF64Fma:
+            e = launch_tma_f64(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st);
+            break;
         case 1: e = launch_tma_f32(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 2: e = launch_tma_f16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 3: e = launch_tma_bf16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
@@ -484,6 +487,7 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
     count_launch();
     switch (storage) {
     case 0: return launch_fast_f64(variant, alpha, dd, g, p, lid_y, st);
+    case kStorageF64Fma: return launch_fast_f64fma(variant, alpha, dd, g, p, lid_y, st);
     case 1: return launch_fast_f32(variant, alpha, dd, g, p, lid_y, st);
     case 2: return launch_fast_f16s(variant, alpha, dd, g, p, lid_y, st);
     case 3: return launch_fast_bf16s(variant, alpha, dd, g, p, lid_y, st);

@@ -82,6 +82,10 @@ constexpr TmaConfig kTmaMenu[kTmaVariants] = {
     {1, 3, 6}, {1, 4, 6}, {2, 2, 8}, {2, 3, 8}, {1, 2, 4}, {4, 2, 8},
 };
 constexpr int kFastVariantCount = kRegisterVariants + kTmaVariants;
+// Storage code of the FP64 step kernels with fused multiply-adds (F64F, built
+// in fast_f64_fma.cu); accepted by launch_fast_step, fast_variant_fits and
+// fast_variant_shape only.  Its bulk-copy variants run the unfused kernels.
+constexpr int kStorageF64Fma = 5;
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
                              int lid_y, int* err, cudaStream_t st);
 // Whether a variant fits this domain (shared memory of the bulk-copy kernels).
@@ -111,6 +115,8 @@ cudaError_t launch_batch_map(const BatchDomain* doms, int ndom, long long vblock
                              cudaStream_t st);
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
+cudaError_t launch_fast_f64fma(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                               cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f16s(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,

@@ -63,7 +63,8 @@ class _Configuration(C.Structure):
 class _Params(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("boundary", C.c_int32 * 6),
                 ("inv_tau", C.c_double), ("lid_velocity", C.c_double), ("gravity", C.c_double * 3),
-                ("device", C.c_int32), ("fast_variant", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("device", C.c_int32), ("fast_variant", C.c_int32), ("fused_multiply_add", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class _Info(C.Structure):
@@ -71,8 +72,8 @@ class _Info(C.Structure):
                 ("vector_cells", C.c_int32), ("step_counter", C.c_int64), ("last_step_was_alpha", C.c_int32),
                 ("fast_path", C.c_int32), ("fast_variant", C.c_int32), ("cells_per_thread", C.c_int32),
                 ("block_threads", C.c_int32), ("beta_cells_per_thread", C.c_int32),
-                ("beta_block_threads", C.c_int32), ("beta_block_exchange", C.c_int32), ("reserved", C.c_int32),
-                ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
+                ("beta_block_threads", C.c_int32), ("beta_block_exchange", C.c_int32),
+                ("fused_multiply_add", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
                 ("device_bytes", C.c_int64)]
 
 
@@ -241,7 +242,8 @@ class CLbmSolverGB300:
 
     def __init__(self, size: Sequence[int], inv_tau: float, lid_velocity: float, storage: str = "f32",
                  boundary: Sequence[int] = (OBSTACLE,) * 6, gravity: Sequence[float] = (0.0, 0.0, 0.0),
-                 device: int = 0, driven_cavity: bool = True, fast_variant: int = -1):
+                 device: int = 0, driven_cavity: bool = True, fast_variant: int = -1,
+                 fused_multiply_add: bool = False):
         self._lib = load_library()
         p = _Params()
         p.size[:] = [int(s) for s in size]
@@ -252,6 +254,7 @@ class CLbmSolverGB300:
         p.gravity[:] = [float(g) for g in gravity]
         p.device = int(device)
         p.fast_variant = 0 if fast_variant < 0 else int(fast_variant) + 1
+        p.fused_multiply_add = 1 if fused_multiply_add else 0
         h = C.c_void_p()
         _check(self._lib.lbm_create(C.byref(p), C.byref(h)))
         self._h = h

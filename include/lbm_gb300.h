@@ -171,7 +171,18 @@ typedef struct lbm_params {
                                    variant v of the vectorised kernels,
                                    v < lbm_fast_variant_count(); see
                                    lbm_autotune                                */
-    int32_t reserved[2];        /* zero                                        */
+    int32_t fused_multiply_add; /* FP64 storage only.  0 (default): the
+                                   collision performs the reference CPU
+                                   kernels' unfused IEEE operations (results
+                                   bit-identical to them).  1: the vectorised
+                                   register-variant steps fuse its
+                                   multiply-adds, as the reference's nvcc build
+                                   does: faster on GB300's FP64 units, within
+                                   1e-15 of the reference CUDA kernels after
+                                   1000 steps, no longer bit-identical to the
+                                   CPU kernels.  Flag-array and bulk-copy steps
+                                   stay unfused.                               */
+    int32_t reserved;           /* zero                                        */
 } lbm_params;
 
 typedef struct lbm_solver lbm_solver;   /* opaque */
@@ -193,7 +204,7 @@ typedef struct lbm_info {
     int32_t beta_block_threads;
     int32_t beta_block_exchange;    /* 1: beta exchanges edge elements across
                                        the block (beta_fast_blk)               */
-    int32_t reserved;
+    int32_t fused_multiply_add;     /* lbm_params.fused_multiply_add           */
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */

@@ -70,6 +70,9 @@ def test_status_strings_and_errors_without_device(lib):
     with pytest.raises(LbmError) as ei:
         CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32", boundary=(1, 1, 1, 1, 1, 3))
     assert ei.value.status == 1  # invalid boundary flag, checked before any CUDA call
+    with pytest.raises(LbmError) as ei:
+        CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32", fused_multiply_add=True)
+    assert ei.value.status == 1  # fused multiply-adds are an FP64 option
     if not torch.cuda.is_available():
         with pytest.raises(LbmError) as ei:
             CLbmSolverGB300((8, 8, 8), 1.6, 0.05)

@@ -267,3 +267,24 @@ def test_full_size_384_fp32_steps_match_oracle(gpu, oracle):
         got = s.get_all()
     want, _ = oracle.run_cavity(*n, dtype, itau, lid, 3)
     assert same_bits(got, want)
+
+
+@pytest.mark.parametrize("variant", [3, 8, 11, 12])
+def test_fp64_fused_multiply_add_close_to_oracle(gpu, oracle, variant):
+    """The opt-in FP64 kernels with fused multiply-adds: not bit-identical to
+    the reference CPU kernels any more, but within rounding of them, and the
+    same whatever the register variant (single steps and graph replays)."""
+    _, itau = orc.tau_of(0.032, np.float64)
+    lid = 0.07
+    n, steps = (37, 20, 30), 70
+    want, _ = oracle.run_cavity(*n, np.float64, itau, lid, steps)
+    with solver(n, np.float64, itau, lid, fast_variant=variant, fused_multiply_add=True) as s:
+        s.run(steps)
+        got = s.get_all()
+    with solver(n, np.float64, itau, lid, fast_variant=3, fused_multiply_add=True) as s:
+        for i in range(steps):
+            (s.simulationStepBeta if i & 1 else s.simulationStepAlpha)()
+        one_by_one = s.get_all()
+    assert same_bits(got, one_by_one)
+    assert np.abs(got - want).max() <= 1e-13
+    assert not same_bits(got, want)  # the multiply-adds really are fused

@@ -26,15 +26,18 @@ def refkernels():
     return ref_gpu
 
 
-@pytest.mark.parametrize("storage,dtype,tol", [("f64", np.float64, 1e-12), ("f32", np.float32, 1e-6)])
+@pytest.mark.parametrize("storage,dtype,tol,fma", [("f64", np.float64, 1e-12, False), ("f32", np.float32, 1e-6, False),
+                                                   ("f64", np.float64, 1e-12, True)])
 @pytest.mark.parametrize("n", [(64, 64, 64), (48, 40, 36)])
-def test_velocity_matches_reference_cuda_kernels(gpu, refkernels, storage, dtype, tol, n):
+def test_velocity_matches_reference_cuda_kernels(gpu, refkernels, storage, dtype, tol, fma, n):
+    """Also for FP64 with fused multiply-adds (lbm_params.fused_multiply_add)."""
     from cavityflow_cuda_gb300 import CLbmSolverGB300
 
     steps = 1000
     _, itau = orc.tau_of(0.032, dtype)  # Re = 100 at 64^3 with lid 0.05
     lid = dtype(0.05)
-    with CLbmSolverGB300(n, itau, lid, storage=storage) as s:
+    with CLbmSolverGB300(n, itau, lid, storage=storage, fused_multiply_add=fma) as s:
+        assert s.info()["fused_multiply_add"] == int(fma)
         dd0, flags = s.get_all(), s.flags_all()
         with refkernels.RefGpuCavity(dd0, flags, itau, lid) as ref:
             ref.run(steps)
