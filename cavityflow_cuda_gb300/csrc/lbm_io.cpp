@@ -5,7 +5,7 @@
 //   uint32    version (1)
 //   int32     storage, nx, ny, nz
 //   int64     step counter
-//   int32     last step was alpha, reserved
+//   int32     last step was alpha, FP64 fused multiply-adds (0/1)
 //   double    inv_tau, lid velocity, gravity x, y, z
 //   int32     boundary[6]
 //   uint64    flag bytes, population bytes
@@ -40,7 +40,7 @@ struct CkptHeader {
     uint32_t version;
     int32_t storage, nx, ny, nz;
     int64_t counter;
-    int32_t last_alpha, reserved;
+    int32_t last_alpha, fma;
     double inv_tau, lid_u, gx, gy, gz;
     int32_t boundary[6];
     uint64_t flag_bytes, pop_bytes;
@@ -111,6 +111,7 @@ int lbm_save_checkpoint(lbm_solver* s, const char* path)
     h.nx = g.nx; h.ny = g.ny; h.nz = g.nz;
     h.counter = s->counter;
     h.last_alpha = s->last_alpha ? 1 : 0;
+    h.fma = s->fma ? 1 : 0;
     h.inv_tau = s->p.inv_tau; h.lid_u = s->p.lid_u;
     h.gx = s->p.gx; h.gy = s->p.gy; h.gz = s->p.gz;
     for (int f = 0; f < 6; ++f) h.boundary[f] = s->bc[f];
@@ -141,7 +142,8 @@ static int read_header(FILE* f, const char* path, CkptHeader& h)
     if (std::fread(&h, sizeof(h), 1, f) != 1) return fail(LBM_ERR_IO, "\"%s\": truncated header", path);
     if (std::memcmp(h.magic, kMagic, 16) != 0 || h.version != 1)
         return fail(LBM_ERR_IO, "\"%s\" is not a version-1 checkpoint of this solver", path);
-    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_F16SR || h.nx <= 0 || h.ny <= 0 || h.nz <= 0)
+    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_F16SR || h.nx <= 0 || h.ny <= 0 || h.nz <= 0 ||
+        (h.fma != 0 && h.fma != 1))
         return fail(LBM_ERR_IO, "\"%s\": corrupt header", path);
     const uint64_t cells = (uint64_t)(h.nx + 2) * (h.ny + 2) * (h.nz + 2);
     if (h.flag_bytes != cells || h.pop_bytes != (uint64_t)lbm::Q * cells * (uint64_t)elem_bytes(h.storage))
@@ -197,6 +199,7 @@ int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** ou
     p.lid_velocity = h.lid_u;
     p.gravity[0] = h.gx; p.gravity[1] = h.gy; p.gravity[2] = h.gz;
     p.device = device;
+    p.fused_multiply_add = h.fma;  // resume with the arithmetic that wrote the checkpoint
     lbm_solver* s = nullptr;
     if (int r = lbm_create(&p, &s)) return r;
     if (int r = lbm_load_checkpoint(s, path)) {

@@ -59,6 +59,7 @@ struct Options {
     int storage = LBM_STORAGE_F32;
     int device = 0;
     int fast_variant = -1;
+    bool fma = false;
     bool autotune = false;
     bool vtk_binary = false;
     std::string checkpoint;
@@ -68,7 +69,7 @@ struct Options {
 
 void usage()
 {
-    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--device N]\n"
+    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--fma] [--device N]\n"
                  "                 [--fast-variant V | --autotune] [--vtk-binary]\n"
                  "                 [--checkpoint FILE --checkpoint-every N] [--resume FILE]\n";
 }
@@ -97,6 +98,8 @@ Options parse(int argc, char** argv)
             o.device = std::atoi(value().c_str());
         } else if (a == "--fast-variant") {
             o.fast_variant = std::atoi(value().c_str());
+        } else if (a == "--fma") {
+            o.fma = true;  // FP64: fused multiply-adds (lbm_params.fused_multiply_add)
         } else if (a == "--autotune") {
             o.autotune = true;
         } else if (a == "--vtk-binary") {
@@ -196,6 +199,7 @@ int main(int argc, char** argv)
         for (int d = 0; d < 3; ++d) p.gravity[d] = lat.acceleration[d];
         p.device = opt.device;
         p.fast_variant = opt.fast_variant < 0 ? 0 : opt.fast_variant + 1;
+        p.fused_multiply_add = opt.fma ? 1 : 0;
         check(lbm_create(&p, &solver), "lbm_create");
         check(lbm_set_driven_cavity(solver), "lbm_set_driven_cavity");
     }

@@ -79,13 +79,16 @@ def read_vtk(path):
     return out
 
 
-@pytest.mark.parametrize("storage", ["f64", "f32", "f16s", "bf16s", "f16sr"])
-def test_checkpoint_resume_is_bit_identical(gpu, tmp_path, storage):
+@pytest.mark.parametrize("storage,fma", [("f64", False), ("f32", False), ("f16s", False), ("bf16s", False),
+                                         ("f16sr", False), ("f64", True)])
+def test_checkpoint_resume_is_bit_identical(gpu, tmp_path, storage, fma):
+    """Also for FP64 with fused multiply-adds: the checkpoint records the
+    arithmetic, and a solver created from it resumes with the same."""
     from cavityflow_cuda_gb300 import CLbmSolverGB300
 
     size = (17, 12, 9)
     ck = str(tmp_path / "run.ckpt")
-    with CLbmSolverGB300(size, 1.6, 0.07, storage=storage) as a:
+    with CLbmSolverGB300(size, 1.6, 0.07, storage=storage, fused_multiply_add=fma) as a:
         a.run(37)                       # odd: the populations sit in the alpha convention
         a.save_checkpoint(ck)
         a.run(40)
@@ -93,12 +96,13 @@ def test_checkpoint_resume_is_bit_identical(gpu, tmp_path, storage):
         want_info = a.info()
     with CLbmSolverGB300.from_checkpoint(ck) as b:
         assert b.storage == storage and b.size == size
+        assert b.info()["fused_multiply_add"] == int(fma)
         assert b.info()["step_counter"] == 37 and b.info()["last_step_was_alpha"] == 1
         b.run(40)
         assert same_bits(b.getDensityDistributions(*full(b)), want)
         assert b.info()["step_counter"] == want_info["step_counter"]
     # restoring into an existing solver of the same shape
-    with CLbmSolverGB300(size, 1.6, 0.07, storage=storage) as c:
+    with CLbmSolverGB300(size, 1.6, 0.07, storage=storage, fused_multiply_add=fma) as c:
         c.run(5)
         c.load_checkpoint(ck)
         c.run(40)
