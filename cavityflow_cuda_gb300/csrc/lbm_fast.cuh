@@ -114,30 +114,6 @@ struct Cells {
     bool active;
 };
 
-// From a thread index t over groups x rows x planes of one domain,
-// t = ((z-1) * ny + (y-1)) * G + gi (the batch kernel's virtual blocks).
-template <int CPT>
-__device__ __forceinline__ Cells cells_of_index(const Grid& g, long long t)
-{
-    const int G = (g.nx + CPT - 1) / CPT;
-    const long long total = (long long)G * g.ny * g.nz;
-    Cells c;
-    c.active = t < total;
-    const long long tt = c.active ? t : 0;
-    if (total <= 0xffffffffll) {  // 32-bit division is far cheaper than 64-bit
-        const uint32_t u = (uint32_t)tt, row = u / (uint32_t)G;
-        c.gi = (int)(u - row * (uint32_t)G);
-        c.y = 1 + (int)(row % (uint32_t)g.ny);
-        c.z = 1 + (int)(row / (uint32_t)g.ny);
-    } else {
-        const long long row = tt / G;
-        c.gi = (int)(tt - row * G);
-        c.y = 1 + (int)(row % g.ny);
-        c.z = 1 + (int)(row / g.ny);
-    }
-    return c;
-}
-
 // From an index i over the G * ny groups of plane z (the step kernels' grid:
 // x over a plane's groups, y over planes); divG divides by G.
 __device__ __forceinline__ Cells cells_of_plane(const Grid& g, int G, const FastDiv& divG, uint32_t i, int z)
@@ -575,10 +551,10 @@ namespace lbm {
 // population arrays share one device pool; a packed table gives each its
 // layout, offset, parameters and its range of "virtual blocks" (BLOCK
 // threads x CPT cells each, numbered consecutively over the domains).  A
-// persistent grid walks the virtual blocks; every CTA finds its domain by
-// binary search and runs the same per-thread bodies as the single-domain
-// kernels, so a domain's result does not depend on its neighbours in the
-// batch.
+// persistent grid walks the virtual blocks; a per-kernel map gives each
+// virtual block's domain, and every CTA runs the same per-thread bodies as
+// the single-domain kernels, so a domain's result does not depend on its
+// neighbours in the batch.
 // ---------------------------------------------------------------------------
 struct alignas(16) BatchDomain {
     Grid g;
