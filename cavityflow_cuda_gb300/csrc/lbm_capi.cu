@@ -79,12 +79,12 @@ bool valid_flag(int32_t f)
 constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 
 // Default launch variant per storage (index into kFastMenu), from kernel
-// timings of the 384^3 cavity on GB300: two-warp blocks with the block-wide
-// beta exchange; FP32 with 8-byte vectors in both kernels, FP16 with a 16-byte
-// alpha and an 8-byte beta, BF16 with 16-byte vectors in both, FP16 with
-// stochastic rounding a 16-byte two-warp alpha and an 8-byte four-warp beta
-// (its beta issues the most instructions per byte).  FP64 is bound
-// by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors (one cell).
+// timings of the 384^3 cavity on GB300: two-warp blocks; FP32 with 8-byte
+// vectors in both kernels and beta's shifted windows accessed directly (no
+// exchange), FP16 (both roundings) with a 16-byte alpha and an 8-byte direct
+// beta, BF16 with 16-byte vectors and the block-wide beta exchange.  FP64 is
+// bound by FP64 arithmetic, where the shapes tie; it keeps 8-byte vectors
+// (one cell).
 }  // namespace
 
 // Batches of the seeded 512-cavity workload (edges 16..96) favour two-warp
@@ -105,10 +105,10 @@ int lbm_detail::default_batch_variant(int storage)
 int lbm_detail::default_variant(int storage)
 {
     switch (storage) {
-    case LBM_STORAGE_F32: return 8;
-    case LBM_STORAGE_F16S: return 10;
+    case LBM_STORAGE_F32: return 13;
+    case LBM_STORAGE_F16S: return 15;
     case LBM_STORAGE_BF16S: return 11;
-    case LBM_STORAGE_F16SR: return 12;
+    case LBM_STORAGE_F16SR: return 15;
     default: return 3;
     }
 }
@@ -551,8 +551,10 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     lbm::fast_variant_shape(s->storage, s->variant, false, s->g.nx, info->beta_cells_per_thread,
                             info->beta_block_threads);
     info->fused_multiply_add = s->fma ? 1 : 0;
-    info->beta_block_exchange =
-        s->variant < lbm::kRegisterVariants && lbm::kFastMenu[s->variant].block_exchange ? 1 : 0;
+    info->beta_block_exchange = s->variant >= lbm::kRegisterVariants ? 0
+                                : lbm::kFastMenu[s->variant].direct       ? 2
+                                : lbm::kFastMenu[s->variant].block_exchange ? 1
+                                                                            : 0;
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;

@@ -298,6 +298,114 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     });
 }
 
+// Element-aligned access to a window of CPT storage elements starting `S`
+// elements (+1 or -1) off an aligned CPT-element vector: the window is split
+// into the widest naturally aligned pieces (at most 16 bytes), e.g. for
+// 16-bit elements and CPT 4 at +1: one 2-byte, one 4-byte and one 2-byte
+// access.  Compile-time recursion over the pieces.
+template <class St, int CPT, int S, int E>
+struct Window {
+    using bits = typename St::bits;
+    static constexpr int kEnd = S + CPT;
+    static constexpr int width()
+    {
+        int w = 1;
+        while (2 * w * (int)sizeof(bits) <= 16 && E % (2 * w) == 0 && E + 2 * w <= kEnd) w *= 2;
+        return w;
+    }
+    static constexpr int W = width();
+    using raw = typename RawVec<W * sizeof(bits)>::type;
+    union Piece {
+        raw u;
+        bits b[W];
+    };
+    __device__ static void load(const bits* v, bits (&out)[CPT])
+    {
+        Piece x;
+        x.u = *reinterpret_cast<const raw*>(v + E);
+#pragma unroll
+        for (int i = 0; i < W; ++i) out[E - S + i] = x.b[i];
+        if constexpr (E + W < kEnd) Window<St, CPT, S, E + W>::load(v, out);
+    }
+    __device__ static void store(bits* v, const bits (&in)[CPT])
+    {
+        Piece x;
+#pragma unroll
+        for (int i = 0; i < W; ++i) x.b[i] = in[E - S + i];
+        *reinterpret_cast<raw*>(v + E) = x.u;
+        if constexpr (E + W < kEnd) Window<St, CPT, S, E + W>::store(v, in);
+    }
+};
+
+// Beta step of the CPT cells of group `c` without any exchange between
+// threads: every slot is read and written at the cells' own pull addresses,
+// the c_x = +-1 slots through element-aligned windows (Window).  Each slot
+// element is touched by exactly one thread, as in the exchanging bodies; the
+// halo and padding columns of a row are part of the windows of its end
+// groups, so rows need no special case.
+template <class St, int CPT>
+__device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict__ dd, const Grid& g,
+                                                  const typename St::T inv_tau, const typename St::T lid_u,
+                                                  const int lid_y, const Cells c, const uint32_t step)
+{
+    using T = typename St::T;
+    using bits = typename St::bits;
+    using IO = Vio<St, CPT>;
+    if (!c.active) return;
+    const int gi = c.gi, y = c.y, z = c.z;
+    const int x0 = 1 + gi * CPT;
+    const long long base = g.idx(x0, y, z);
+
+    // p[k][v]: value of slot k at (cell x0+v) + c_k
+    bits p[Q][CPT];
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
+        if constexpr (cx == 0) IO::load_raw(dd + rb, p[k]);
+        else Window<St, CPT, cx, cx>::load(dd + rb, p[k]);
+    });
+
+    const bool lid = (y == lid_y);
+    const T rho0 = St::shifted ? T(0) : T(1);
+    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
+#pragma unroll
+    for (int v = 0; v < CPT; ++v) {
+        if (x0 + v > g.nx) continue;  // halo/padding lane: write back what was read
+        T cc[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) cc[opp(k)] = St::load_step(p[k][v]);
+        if (lid) inject_step<St>(cc, rho0, lid_u);
+        else collide<St>(cc, inv_tau);
+        uint32_t h = 0;
+        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
+#pragma unroll
+        for (int k = 0; k < Q; ++k) p[k][v] = store_pop<St>(cc[k], h, k);  // population k -> slot k at x + c_k
+    }
+
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
+        if constexpr (cx == 0) IO::store_raw(dd + rb, p[k]);
+        else Window<St, CPT, cx, cx>::store(dd + rb, p[k]);
+    });
+}
+
+template <class St, int CPT, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) beta_fast_direct(typename St::bits* __restrict__ dd, const Grid g,
+                                                                const typename St::T inv_tau,
+                                                                const typename St::T lid_u, const int lid_y,
+                                                                const uint32_t* __restrict__ step_base,
+                                                                const uint32_t step_off, const FastDiv divG,
+                                                                const int z_base)
+{
+    const int G = (g.nx + CPT - 1) / CPT;
+    beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+                               cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
+                               step_of<St>(step_base, step_off));
+}
+
 // Beta step with the neighbour exchange done block-wide: inside a warp by
 // shuffles, across the warps of a block through shared memory (two block
 // barriers), so only lanes at a row edge or at the block's two ends touch the
@@ -521,7 +629,8 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
     }
     constexpr KernelShape k = fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    if constexpr (fv.block_exchange) return launch(beta_fast_blk<St, CPT, k.block, k.minb>, CPT, k.block);
+    if constexpr (fv.direct) return launch(beta_fast_direct<St, CPT, k.block, k.minb>, CPT, k.block);
+    else if constexpr (fv.block_exchange) return launch(beta_fast_blk<St, CPT, k.block, k.minb>, CPT, k.block);
     else return launch(beta_fast<St, CPT, k.block, k.minb>, CPT, k.block);
 }
 
@@ -617,7 +726,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // publishes it and keeps the other buffer from being overwritten while read.
 // Every thread of a CTA walks the same virtual blocks, so that barrier and
 // the block-wide barriers of the exchanging beta body are reached uniformly.
-template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, bool kExchange>
+// kBeta: 0 warp exchange (beta_cells), 1 block exchange (beta_cells_blk),
+// 2 direct windows (beta_cells_direct).
+template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, int kBeta>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
                                                           const BatchDomain* __restrict__ doms,
                                                           const int* __restrict__ vb_dom,
@@ -651,7 +762,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         const Cells c = cells_of_vblock(d, which, (uint32_t)(vb - d.block_start[which]) * BLOCK + threadIdx.x);
         const uint32_t ds = step + d.step0;
         if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
-        else if constexpr (kExchange)
+        else if constexpr (kBeta == 2)
+            beta_cells_direct<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
+        else if constexpr (kBeta == 1)
             beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
         else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
     }
@@ -663,7 +776,7 @@ cudaError_t launch_batch_kernel(const BatchArgs& a, cudaStream_t st)
     constexpr FastVariant fv = kFastMenu[VARIANT];
     constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha, fv.block_exchange>;
+    auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha, fv.direct ? 2 : fv.block_exchange ? 1 : 0>;
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

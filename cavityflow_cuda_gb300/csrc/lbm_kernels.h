@@ -51,12 +51,17 @@ struct KernelShape {
 // exchanges the odd element of its shifted slots either inside each warp
 // (shuffles; warp-edge lanes use scalar accesses) or across the whole block
 // (shuffles plus shared memory; only block- and row-edge lanes do).
+// With `direct`, beta exchanges nothing: each thread loads and stores the
+// one-cell-shifted windows of the c_x = +-1 slots itself with element-aligned
+// accesses (2-4 per window), so there are no shuffles, shared memory or
+// barriers and no row- or block-edge cases.
 struct FastVariant {
     KernelShape alpha;
     KernelShape beta;
     bool block_exchange;
+    bool direct = false;
 };
-constexpr int kRegisterVariants = 13;
+constexpr int kRegisterVariants = 18;
 constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
     {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
@@ -71,6 +76,11 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 64, 4}, {2, 64, 8}, true},     // alpha 16-byte, beta 8-byte vectors, block exchange
     {{1, 64, 4}, {1, 64, 4}, true},     // 16-byte vectors, two-warp blocks, block exchange
     {{1, 64, 4}, {2, 128, 4}, true},    // alpha 16-byte two-warp, beta 8-byte four-warp blocks
+    {{2, 64, 8}, {2, 64, 8}, false, true},    // 8-byte vectors, two-warp blocks, direct shifted windows
+    {{2, 128, 4}, {2, 128, 4}, false, true},  // 8-byte vectors, four-warp blocks, direct
+    {{1, 64, 4}, {2, 64, 8}, false, true},    // alpha 16-byte, beta 8-byte, direct
+    {{1, 64, 4}, {1, 64, 4}, false, true},    // 16-byte vectors, two-warp blocks, direct
+    {{2, 256, 2}, {2, 256, 2}, false, true},  // 8-byte vectors, eight-warp blocks, direct
 };
 struct TmaConfig {
     int rows;            // rows per work unit

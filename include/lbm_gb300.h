@@ -202,8 +202,10 @@ typedef struct lbm_info {
     int32_t block_threads;      /* threads per block of its alpha kernel       */
     int32_t beta_cells_per_thread;  /* the same for its beta kernel            */
     int32_t beta_block_threads;
-    int32_t beta_block_exchange;    /* 1: beta exchanges edge elements across
-                                       the block (beta_fast_blk)               */
+    int32_t beta_block_exchange;    /* how beta gets the one-cell-shifted
+                                       slots: 0 warp shuffles (beta_fast), 1
+                                       across the block (beta_fast_blk), 2 no
+                                       exchange (beta_fast_direct)             */
     int32_t fused_multiply_add;     /* lbm_params.fused_multiply_add           */
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
@@ -267,11 +269,11 @@ int lbm_synchronize(lbm_solver* solver);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: 13 register-blocked
- * vector kernels (0..12: cells per thread, threads per block and blocks per
+/* Number of launch variants of the box-cavity kernels: 18 register-blocked
+ * vector kernels (0..17: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
- * elements per warp or per block) and 6 row-pipelined bulk-copy kernels
- * (13..18: rows per unit, buffers, consumer warps). */
+ * elements per warp, per block or not at all) and 6 row-pipelined bulk-copy
+ * kernels (18..23: rows per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Number of register variants (the first variants; the batch kernel's menu). */
 int lbm_register_variant_count(void);

@@ -117,7 +117,7 @@ def test_cli_usage_and_argument_errors(lib, tmp_path):
 
 
 def test_launch_variant_menu_size(lib):
-    """13 register variants (0-12) and 6 bulk-copy variants (13-18); the GPU
+    """18 register variants (0-17) and 6 bulk-copy variants (18-23); the GPU
     parity tests enumerate exactly these."""
-    assert lib.lbm_fast_variant_count() == 19
-    assert lib.lbm_register_variant_count() == 13
+    assert lib.lbm_fast_variant_count() == 24
+    assert lib.lbm_register_variant_count() == 18

@@ -30,7 +30,7 @@ def test_batch_domains_match_single_solvers(gpu, storage):
         assert np.array_equal(got[i].view(np.uint8), want.view(np.uint8)), (storage, i, size)
 
 
-@pytest.mark.parametrize("variant", range(13))
+@pytest.mark.parametrize("variant", range(18))
 def test_batch_every_variant(gpu, variant):
     from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmBatch
 
@@ -58,7 +58,7 @@ def test_batch_views_getters_and_guards(gpu):
             assert np.array_equal(v.getVelocities(), s.getVelocities())
             assert np.allclose(v.reduce(), s.reduce(), rtol=1e-12)
         best, ms = b.autotune(pairs=2)
-        assert 0 <= best < 13 and b.info()["step_counter"] == 10
+        assert 0 <= best < 18 and b.info()["step_counter"] == 10
         v.simulationStepAlpha()          # a domain leaves the batch's time level
         with pytest.raises(LbmError):
             b.run(2)

@@ -91,12 +91,13 @@ def test_odd_shapes_match_oracle(gpu, oracle, dtype, n, steps):
         assert same_bits(s.get_all(), want)
 
 
-@pytest.mark.parametrize("variant", range(19))
+@pytest.mark.parametrize("variant", range(24))
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_every_launch_variant_matches_oracle(gpu, oracle, variant, dtype):
-    """Each launch variant: register-blocked vector kernels (0-11; 8-11 with
+    """Each launch variant: register-blocked vector kernels (0-17; 8-12 with
     the block-wide beta exchange, whose blocks here straddle rows (37 cells)
-    and split them (300 cells)) and the row-pipelined bulk-copy kernels (12-17)."""
+    and split them (300 cells); 13-17 with direct shifted windows) and the
+    row-pipelined bulk-copy kernels (18-23)."""
     _, itau = orc.tau_of(0.032, dtype)
     lid = dtype(0.07)
     from cavityflow_cuda_gb300 import LbmError
