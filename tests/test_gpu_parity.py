@@ -91,6 +91,20 @@ def test_odd_shapes_match_oracle(gpu, oracle, dtype, n, steps):
         assert same_bits(s.get_all(), want)
 
 
+@pytest.mark.parametrize("variant", [3, 8, 13, 15])
+@pytest.mark.parametrize("n", [(3, 2, 70000), (70000, 2, 3), (2, 70000, 3)])
+def test_extreme_aspect_ratios_match_oracle(gpu, oracle, variant, n):
+    """More planes than one launch's grid holds (the step kernels launch the
+    planes in chunks of 65535), and rows or columns of 70000 cells."""
+    _, itau = orc.tau_of(0.0192, np.float32)
+    lid = np.float32(0.08)
+    steps = 5
+    want, _ = oracle.run_cavity(*n, np.float32, itau, lid, steps)
+    with solver(n, np.float32, itau, lid, fast_variant=variant) as s:
+        s.run(steps)
+        assert same_bits(s.get_all(), want), (variant, n)
+
+
 @pytest.mark.parametrize("variant", range(24))
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_every_launch_variant_matches_oracle(gpu, oracle, variant, dtype):
