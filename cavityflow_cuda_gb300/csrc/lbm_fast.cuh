@@ -18,6 +18,11 @@
 //                  block (shuffles inside a warp, shared memory between
 //                  warps), so that only the block's two end lanes and row
 //                  edges use scalar accesses.
+//   beta_fast_direct -- the same step with no exchange at all: each thread
+//                  reads and writes its own one-cell-shifted windows with
+//                  element-aligned pieces (the default for FP32 and FP16).
+//   batch_step  -- the persistent kernel of a batch of cavities, running the
+//                  same per-thread bodies over a packed domain table.
 //
 // Template parameters: St storage type, CPT cells per thread (one vector of
 // CPT elements per slot: 16, 8 or 4 bytes), BLOCK threads per block, MINB the
