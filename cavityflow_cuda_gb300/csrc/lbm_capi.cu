@@ -679,6 +679,17 @@ int lbm_synchronize(lbm_solver* s)
     return check_kernel_flag(s);
 }
 
+int lbm_selftest_bounded_wait(lbm_solver* s, int32_t limit_us)
+{
+    if (int r = check_solver(s)) return r;
+    if (limit_us < 1 || limit_us > 2000000) return fail(LBM_ERR_INVALID_ARGUMENT, "limit_us must be in [1, 2000000]");
+    CK(cudaSetDevice(s->device), "cudaSetDevice");
+    CK(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+    if (int r = check_kernel_flag(s)) return r;  // an earlier failure is reported as such
+    CK(lbm::launch_bounded_wait_probe(err_flag(s), (uint64_t)limit_us * 1000u, 0), "bounded wait probe launch");
+    return lbm_synchronize(s);
+}
+
 int lbm_fast_variant_count(void) { return lbm::kFastVariantCount; }
 int lbm_register_variant_count(void) { return lbm::kRegisterVariants; }
 

@@ -31,6 +31,9 @@ cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned lo
 // word at step_base set to its first step before each replay.
 inline bool storage_stochastic(int storage) { return storage == 4; }
 cudaError_t launch_set_step(uint32_t* word, uint32_t value, cudaStream_t st);
+// One block waiting on an mbarrier that nothing arrives at, bounded by
+// limit_ns; raises bit 1 of *err when it gives up (lbm_selftest_bounded_wait).
+cudaError_t launch_bounded_wait_probe(int* err, uint64_t limit_ns, cudaStream_t st);
 // Box-cavity step.  Variants 0..kRegisterVariants-1 index kFastMenu, the
 // register kernels of lbm_fast.cuh; the rest index kTmaMenu, the
 // row-pipelined bulk-copy kernels of lbm_tma.cuh.  A variant that does not

@@ -84,11 +84,11 @@ __device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
 constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
 
 // Waits until the phase with `parity` of `bar` has completed; false if the
-// time limit passes first.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+// time limit (nanoseconds) passes first.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns = kWaitLimitNs)
 {
     if (mbar_test(bar, parity)) return true;
-    const uint64_t deadline = now_ns() + kWaitLimitNs;
+    const uint64_t deadline = now_ns() + limit_ns;
     for (;;) {
         if (mbar_test(bar, parity)) return true;
         if (now_ns() > deadline) return false;

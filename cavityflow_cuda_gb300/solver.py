@@ -107,6 +107,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "lbm_step_beta_cuboid": ([V, P, P, P], I),
         "lbm_run": ([V, I64, P], I),
         "lbm_synchronize": ([V], I),
+        "lbm_selftest_bounded_wait": ([V, C.c_int32], I),
         "lbm_fast_variant_count": ([], I),
         "lbm_register_variant_count": ([], I),
         "lbm_set_fast_variant": ([V, C.c_int32], I),

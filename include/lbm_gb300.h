@@ -263,8 +263,17 @@ int lbm_step_beta_cuboid(lbm_solver* solver, const int32_t origin[3], const int3
  * graph of captured alpha/beta pairs. */
 int lbm_run(lbm_solver* solver, int64_t steps, void* stream);
 
-/* Waits for all work queued by the solver. */
+/* Waits for all work queued by the solver.  LBM_ERR_TIMEOUT if one of its
+ * kernels gave up a bounded device-side wait (the solver stays usable). */
 int lbm_synchronize(lbm_solver* solver);
+
+/* Diagnostics of that failure path, with no GPU fault: runs on the solver's
+ * device one block that waits on an mbarrier nothing arrives at, with the
+ * bulk-copy kernels' bounded wait (limit_us in [1, 2000000] microseconds
+ * instead of their 2 s), raising the solver's error flag when it gives up;
+ * then synchronises.  Returns LBM_ERR_TIMEOUT, after which the solver's
+ * state and later steps are unaffected. */
+int lbm_selftest_bounded_wait(lbm_solver* solver, int32_t limit_us);
 
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
