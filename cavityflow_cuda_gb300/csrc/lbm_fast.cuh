@@ -766,12 +766,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         const BatchDomain& d = desc[buf];
         const Cells c = cells_of_vblock(d, which, (uint32_t)(vb - d.block_start[which]) * BLOCK + threadIdx.x);
         const uint32_t ds = step + d.step0;
-        if constexpr (kAlpha) alpha_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
-        else if constexpr (kBeta == 2)
-            beta_cells_direct<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
-        else if constexpr (kBeta == 1)
-            beta_cells_blk<St, CPT, BLOCK>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
-        else beta_cells<St, CPT>(pool + d.offset, d.g, T(d.inv_tau), T(d.lid_u), d.lid_y, c, ds);
+        const Grid g = d.g;  // in registers for the body (its barriers would force shared-memory reloads)
+        typename St::bits* const dd = pool + d.offset;
+        const T inv_tau = T(d.inv_tau), lid_u = T(d.lid_u);
+        const int lid_y = d.lid_y;
+        if constexpr (kAlpha) alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
+        else if constexpr (kBeta == 2) beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
+        else if constexpr (kBeta == 1) beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, c, ds);
+        else beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
     }
 }
 
