@@ -117,3 +117,30 @@ def test_fp16_velocity_error_against_fp64(gpu):
     assert errs["f16s"] < 1e-3, errs
     assert errs["f16sr"] < errs["f16s"], errs  # stochastic rounding removes the bias of rounding to nearest
     print("L2 velocity error vs FP64:", errs)
+
+
+@pytest.mark.parametrize("storage", ["f16s", "bf16s", "f16sr"])
+def test_shifted_flag_array_path_matches_oracle(gpu, oracle, storage):
+    """16-bit storage through the flag-array kernels: an interior obstacle,
+    the lid, whole-domain and cuboid steps (each keyed by the solver's step
+    count for stochastic rounding), bit for bit against the oracle."""
+    _, itau = orc.tau_of(0.0192, np.float32)
+    lid = np.float32(0.08)
+    n = (14, 12, 10)
+    kind = KIND[storage]
+    dd, flags = oracle.init_s(*n)
+    oracle.set_lid(flags)
+    flags[4:7, 5:8, 3:9] = orc.OBSTACLE
+    halo = (n[0] + 2, n[1] + 2, n[2] + 2)
+    seq = [(None, None)] * 4 + [((1, 1, 1), (7, 12, 10)), ((8, 1, 1), (7, 12, 10)),
+                                ((0, 0, 0), halo), ((2, 3, 4), (9, 8, 5))] + [(None, None)] * 3
+    with shifted_solver(n, storage, itau, lid, driven_cavity=False) as s:
+        s.setFlags(flags, (0, 0, 0), halo)
+        assert s.info()["fast_path"] == 0
+        for i, (o, sz) in enumerate(seq):
+            step = s.simulationStepBeta if i & 1 else s.simulationStepAlpha
+            step(o, sz) if o is not None else step()
+            oracle.step_s(dd, flags, i, itau, lid, kind, origin=o, size=sz)
+        got = s.get_all()
+    want = oracle.unshift(dd, kind)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), storage
