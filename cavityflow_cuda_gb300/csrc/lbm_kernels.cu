@@ -218,6 +218,37 @@ __global__ void compute_macros(const typename St::bits* __restrict__ dd, const u
     }
 }
 
+// The same density and velocity for a box cavity with obstacle walls and the
+// lid on plane y = ny (the geometry of a solver after set_driven_cavity),
+// taken from the geometry rather than a flag array, for interior cells only,
+// packed x fastest: out[0..n) rho, then jx, jy, jz planes of n = nx*ny*nz.
+// `out` may be mapped host memory.
+template <class St>
+__global__ void compute_macros_cavity(const typename St::bits* __restrict__ dd, const Grid g,
+                                      const bool last_alpha, const typename St::T lid_u,
+                                      typename St::T* __restrict__ out)
+{
+    using T = typename St::T;
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x = 1 + (int)(i % g.nx);
+        const int y = 1 + (int)((i / g.nx) % g.ny);
+        const int z = 1 + (int)(i / ((long long)g.nx * g.ny));
+        T r = T(1), vx = lid_u, vy = T(0), vz = T(0);
+        if (y != g.ny) {
+            T f[Q];
+            post_populations<St>(dd, g, x, y, z, last_alpha, f);
+            moments(f, r, vx, vy, vz);
+            if (St::shifted) r = r + T(1);
+        }
+        out[i] = r;
+        out[n + i] = vx;
+        out[2 * n + i] = vy;
+        out[3 * n + i] = vz;
+    }
+}
+
 // FP64 mass and momentum, pass 1: one partial sum per block (warp shuffles,
 // then a fixed-order combine of the warps), so the result is deterministic.
 // Mass counts every live slot: the 19 own slots of each active (FLUID or
@@ -362,6 +393,17 @@ long long kernel_launches() { return __atomic_load_n(&g_launches, __ATOMIC_RELAX
 void add_launches(long long n) { __atomic_fetch_add(&g_launches, n, __ATOMIC_RELAXED); }
 
 static void count_launch(int n = 1) { add_launches(n); }
+
+cudaError_t launch_init_populations(int storage, void* dd, const Grid& g, cudaStream_t st)
+{
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        init_populations<St><<<grid_for((long long)Q * g.S, 256, 4096), 256, 0, st>>>(
+            static_cast<typename St::bits*>(dd), g);
+        return cudaGetLastError();
+    });
+}
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st)
 {
@@ -522,6 +564,19 @@ cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, con
         using T = typename St::T;
         compute_macros<St><<<grid_for(g.cells(), 256, 8192), 256, 0, st>>>(
             static_cast<const typename St::bits*>(dd), flags, g, last_alpha, T(lid_u), static_cast<T*>(out));
+        return cudaGetLastError();
+    });
+}
+
+cudaError_t launch_macros_cavity(int storage, const void* dd, const Grid& g, bool last_alpha, double lid_u,
+                                 void* out, cudaStream_t st)
+{
+    count_launch();
+    return with_storage(storage, [&](auto tag) {
+        using St = decltype(tag);
+        using T = typename St::T;
+        compute_macros_cavity<St><<<grid_for((long long)g.nx * g.ny * g.nz, 256, 8192), 256, 0, st>>>(
+            static_cast<const typename St::bits*>(dd), g, last_alpha, T(lid_u), static_cast<T*>(out));
         return cudaGetLastError();
     });
 }

@@ -25,6 +25,8 @@ long long kernel_launches();
 void add_launches(long long n);
 
 cudaError_t launch_init(int storage, void* dd, uint8_t* flags, const Grid& g, const Bc& bc, cudaStream_t st);
+// Populations at rest only (no flag array).
+cudaError_t launch_init_populations(int storage, void* dd, const Grid& g, cudaStream_t st);
 cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned long long* counts, cudaStream_t st);
 // Storage types whose step kernels round stochastically, keyed by the step
 // (Params::step_base/step_off); a graph replaying such launches needs the
@@ -152,6 +154,11 @@ cudaError_t launch_general_step(int storage, bool alpha, void* dd, const uint8_t
                                 const Params& p, int3 origin, int3 size, cudaStream_t st);
 cudaError_t launch_macros(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
                           double lid_u, void* out, cudaStream_t st);
+// Interior density and velocity of a box cavity with the lid on y = ny, from
+// the geometry; packed x fastest (rho, jx, jy, jz planes); `out` may be
+// mapped host memory.
+cudaError_t launch_macros_cavity(int storage, const void* dd, const Grid& g, bool last_alpha, double lid_u,
+                                 void* out, cudaStream_t st);
 int reduce_blocks(const Grid& g);
 cudaError_t launch_reduce(int storage, const void* dd, const uint8_t* flags, const Grid& g, bool last_alpha,
                           double* partials, double* out, cudaStream_t st);

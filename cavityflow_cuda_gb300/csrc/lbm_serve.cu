@@ -5,16 +5,20 @@
 // in a FIFO queue.  Each round the server
 //   1. admits queued requests, in order, while their populations fit the
 //      device arena (a first-fit allocator over one allocation sized to the
-//      memory budget) and their per-request metadata fits what is left of the
-//      budget; an admitted request is a solver view on its arena block,
-//      initialised at rest with the lid set;
+//      memory budget); an admitted request is its arena block of populations,
+//      initialised at rest by one kernel on the server's stream (the walls and
+//      the lid come from the geometry, so a request has no flag array);
 //   2. advances every resident request by the same even number of steps with
 //      the batch kernel over a packed table of the resident domains (sized so
 //      the round lasts about the target time), or, when some request has a
 //      single step left, runs that last alpha step for those requests alone;
-//   3. retires finished requests: density and velocity of the last collided
-//      time level are copied to host memory, the arena block is freed and a
-//      completion is posted.
+//   3. retires finished requests: one kernel per request writes density and
+//      velocity of the last collided time level straight into mapped pinned
+//      host memory, one stream synchronisation covers them all, then the
+//      arena blocks are freed and completions posted.
+// Admission and retirement allocate no device memory and make no
+// device-wide synchronisation, so the GPU idles only for the host work of
+// packing the next round's table.
 // Requests that arrive while others are on the GPU therefore join the next
 // round's launches as memory frees up, and their work shares the device with
 // the requests already running.  Each request's populations evolve exactly as
@@ -22,6 +26,7 @@
 // single-domain one).  One host thread drives a server.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -44,16 +49,23 @@ namespace {
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-constexpr double kArenaShare = 0.95;   // of the budget, for populations; the rest for per-request metadata
+constexpr double kArenaShare = 0.95;   // of the budget, for populations; the rest for the table and block maps
 constexpr size_t kAlign = 256;
+constexpr size_t kStageChunk = (size_t)1 << 30;  // host staging of one retirement batch, unless one result is larger
+
+struct Request;
+struct Staged {
+    Request* r;
+    size_t at;  // byte offset in its staging buffer
+};
 
 struct Request {
     int64_t id = 0;
     lbm_request spec{};
     double submit_t = 0, admit_t = -1, finish_t = -1;
     int64_t remaining = 0;
-    size_t offset = 0, bytes = 0, meta_bytes = 0;
-    lbm_solver* view = nullptr;
+    size_t offset = 0, bytes = 0;
+    lbm::Grid g{};
     int status = LBM_OK;
     std::vector<unsigned char> rho, u;
 };
@@ -113,7 +125,6 @@ struct lbm_server {
     char* arena = nullptr;
     size_t arena_bytes = 0;
     Arena alloc;
-    size_t meta_in_use = 0;
     size_t peak_bytes = 0;
     std::deque<Request*> queue;
     std::vector<Request*> active;
@@ -125,6 +136,14 @@ struct lbm_server {
     int* vb_map[2] = {nullptr, nullptr};  // domain of each virtual block, per kernel
     long long vb_cap[2] = {0, 0};
     uint32_t* zero_word = nullptr;  // step base of the round launches (a request's step is its own count)
+    // Results go to mapped pinned host memory, two buffers used in turn: the
+    // kernels of one round write buffer `cur` while the host copies the
+    // previous round's results out of the other.
+    char* stage[2] = {nullptr, nullptr};
+    void* stage_dev[2] = {nullptr, nullptr};  // their device addresses
+    size_t stage_cap[2] = {0, 0};
+    int cur = 0;
+    std::vector<Staged> staged;  // results in stage[cur ^ 1] not yet copied out
     cudaStream_t stream = nullptr;
     int64_t next_id = 1;
     int64_t completed = 0;
@@ -148,69 +167,37 @@ size_t population_bytes(const int32_t size[3], int storage)
     return ((size_t)lbm::Q * g.S * elem_bytes(storage) + kAlign - 1) / kAlign * kAlign;
 }
 
-// Device bytes a solver view needs besides its populations (flags, reduction
-// scratch, counters), as create_solver allocates them.
-size_t metadata_bytes(const int32_t size[3])
+// Host bytes of a request's result: density and three velocity components of
+// every interior cell.
+size_t result_bytes(const Request* r, int storage)
 {
-    const size_t cells = (size_t)(size[0] + 2) * (size[1] + 2) * (size[2] + 2);
-    return cells + (4 * (size_t)lbm::kReduceMaxBlocks + 4) * sizeof(double) + 64;
+    return (size_t)4 * r->spec.size[0] * r->spec.size[1] * r->spec.size[2] * (size_t)value_bytes(storage);
 }
 
 void free_request(lbm_server* s, Request* r)
 {
-    if (r->view) {
-        destroy_solver(r->view);
-        r->view = nullptr;
-    }
     if (r->bytes) {
         s->alloc.release(r->offset, r->bytes);
         r->bytes = 0;
-    }
-    if (r->meta_bytes) {
-        s->meta_in_use -= r->meta_bytes;
-        r->meta_bytes = 0;
     }
 }
 
 int admit(lbm_server* s)
 {
-    const size_t meta_budget = (size_t)s->cfg.budget_bytes - s->arena_bytes;
     while (!s->queue.empty()) {
         Request* r = s->queue.front();
         const size_t bytes = population_bytes(r->spec.size, s->cfg.storage);
-        const size_t meta = metadata_bytes(r->spec.size);
-        if (s->meta_in_use + meta > meta_budget) break;
         size_t off = 0;
         if (!s->alloc.alloc(bytes, off)) break;  // strict FIFO: the head waits for memory
         s->queue.pop_front();
         r->offset = off;
         r->bytes = bytes;
-        r->meta_bytes = meta;
-        s->meta_in_use += meta;
-        lbm_params p;
-        std::memset(&p, 0, sizeof(p));
-        for (int d = 0; d < 3; ++d) p.size[d] = r->spec.size[d];
-        p.storage = s->cfg.storage;
-        for (int f = 0; f < 6; ++f) p.boundary[f] = LBM_OBSTACLE;
-        p.inv_tau = r->spec.inv_tau;
-        p.lid_velocity = r->spec.lid_velocity;
-        p.device = s->cfg.device;
-        p.fast_variant = s->variant + 1;
-        int rc = create_solver(&p, s->arena + off, &r->view);
-        if (rc == LBM_OK) rc = lbm_set_driven_cavity(r->view);
-        if (rc != LBM_OK) {
-            r->status = rc;
-            free_request(s, r);
-            r->finish_t = s->now();
-            s->finished[r->id] = r;
-            s->completions.push_back({r->id, r->spec.steps, 0, rc, 0, r->submit_t, r->admit_t, r->finish_t});
-            continue;
-        }
+        // populations at rest; the steps that follow on the same stream see them
+        CK(lbm::launch_init_populations(s->cfg.storage, s->arena + off, r->g, s->stream), "server init launch");
         r->admit_t = s->now();
         r->remaining = r->spec.steps;
         s->active.push_back(r);
-        const size_t in_use = s->alloc.used() + s->meta_in_use;
-        s->peak_bytes = std::max(s->peak_bytes, in_use);
+        s->peak_bytes = std::max(s->peak_bytes, s->alloc.used());
     }
     return LBM_OK;
 }
@@ -221,14 +208,14 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&v
     s->table.resize(reqs.size());
     long long next[2] = {0, 0};
     for (size_t i = 0; i < reqs.size(); ++i) {
-        const lbm_solver* v = reqs[i]->view;
+        const Request* r = reqs[i];
         lbm::BatchDomain& d = s->table[i];
         std::memset(&d, 0, sizeof(d));
-        d.g = v->g;
-        d.offset = (long long)(reqs[i]->offset / (size_t)elem_bytes(s->cfg.storage));
-        d.inv_tau = v->p.inv_tau;
-        d.lid_u = v->p.lid_u;
-        d.lid_y = v->g.ny;
+        d.g = r->g;
+        d.offset = (long long)(r->offset / (size_t)elem_bytes(s->cfg.storage));
+        d.inv_tau = r->spec.inv_tau;
+        d.lid_u = r->spec.lid_velocity;
+        d.lid_y = r->g.ny;
         d.step0 = (uint32_t)(reqs[i]->spec.steps - reqs[i]->remaining);  // steps this request has taken
         for (int kind = 0; kind < 2; ++kind) {  // alpha, beta kernel
             int cpt = 1, block = 1;
@@ -267,26 +254,84 @@ int upload_table(lbm_server* s, const std::vector<Request*>& reqs, long long (&v
     return LBM_OK;
 }
 
-int retire(lbm_server* s, Request* r)
+size_t round_up(size_t bytes) { return (bytes + kAlign - 1) / kAlign * kAlign; }
+
+// Makes staging buffer b hold at least `bytes`; it holds no results that
+// are still to be copied out.
+int reserve_stage(lbm_server* s, int b, size_t bytes)
 {
-    lbm_solver* v = r->view;
-    v->counter = r->spec.steps;
-    v->last_alpha = (r->spec.steps & 1) != 0;
-    v->macros_fresh = false;
-    const size_t cells = (size_t)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
-    const size_t vb = (size_t)value_bytes(s->cfg.storage);
-    r->rho.resize(cells * vb);
-    r->u.resize(3 * cells * vb);
-    int rc = lbm_get_densities(v, nullptr, nullptr, r->rho.data());
-    if (rc == LBM_OK) rc = lbm_get_velocities(v, nullptr, nullptr, r->u.data());
-    r->status = rc;
+    if (bytes <= s->stage_cap[b]) return LBM_OK;
+    CK(cudaStreamSynchronize(s->stream), "server staging");
+    if (s->stage[b]) cudaFreeHost(s->stage[b]);
+    s->stage[b] = nullptr;
+    s->stage_dev[b] = nullptr;
+    s->stage_cap[b] = 0;
+    const size_t cap = round_up(bytes);
+    CK(cudaHostAlloc((void**)&s->stage[b], cap, cudaHostAllocMapped), "cudaHostAlloc server staging");
+    s->stage_cap[b] = cap;
+    CK(cudaHostGetDevicePointer(&s->stage_dev[b], s->stage[b], 0), "cudaHostGetDevicePointer server staging");
+    return LBM_OK;
+}
+
+// Queues on the server's stream the kernels that write the results of
+// done[first], done[first + 1], ... into staging buffer b from its start, as
+// many as fit (the first always does: the buffer holds the largest result);
+// `next` follows the first request not queued, also when a launch fails.  A result is density and
+// velocity of the time level collided last: after alpha for an odd step count.
+int stage_results(lbm_server* s, int b, const std::vector<Request*>& done, size_t first,
+                  std::vector<Staged>& staged, size_t& next)
+{
+    size_t used = 0;
+    for (next = first; next < done.size(); ++next) {
+        const Request* r = done[next];
+        const size_t bytes = round_up(result_bytes(r, s->cfg.storage));
+        if (next > first && used + bytes > s->stage_cap[b]) break;
+        CK(lbm::launch_macros_cavity(s->cfg.storage, s->arena + r->offset, r->g, (r->spec.steps & 1) != 0,
+                                     r->spec.lid_velocity, static_cast<char*>(s->stage_dev[b]) + used, s->stream),
+           "server result launch");
+        staged.push_back({done[next], used});
+        used += bytes;
+    }
+    return LBM_OK;
+}
+
+void complete(lbm_server* s, Request* r, int status)
+{
+    r->status = status;
     free_request(s, r);
     r->finish_t = s->now();
-    s->completed += 1;
+    if (status == LBM_OK) s->completed += 1;
     s->finished[r->id] = r;
+    const int64_t cells = (int64_t)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
     s->completions.push_back(
-        {r->id, r->spec.steps, (int64_t)cells, rc, 0, r->submit_t, r->admit_t, r->finish_t});
-    return LBM_OK;
+        {r->id, r->spec.steps, status == LBM_OK ? cells : 0, status, 0, r->submit_t, r->admit_t, r->finish_t});
+}
+
+// Copies results whose kernels have completed out of staging buffer b and
+// posts their completions.
+void post_staged(lbm_server* s, int b, std::vector<Staged>& staged)
+{
+    const size_t vb = (size_t)value_bytes(s->cfg.storage);
+    for (const Staged& e : staged) {
+        Request* r = e.r;
+        const size_t cells = (size_t)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+        const char* src = s->stage[b] + e.at;
+        r->rho.assign(src, src + cells * vb);
+        r->u.assign(src + cells * vb, src + 4 * cells * vb);
+        complete(s, r, LBM_OK);
+    }
+    staged.clear();
+}
+
+// Moves the active requests with no steps left to `done`, in order.
+void take_finished(lbm_server* s, std::vector<Request*>& done)
+{
+    size_t keep = 0;
+    for (Request* r : s->active) {
+        if (r->remaining == 0) done.push_back(r);
+        else s->active[keep++] = r;
+    }
+    s->active.resize(keep);
 }
 
 }  // namespace
@@ -343,6 +388,9 @@ int lbm_server_destroy(lbm_server* s)
         free_request(s, r);
         delete r;
     }
+    for (const Staged& e : s->staged) delete e.r;
+    for (int b = 0; b < 2; ++b)
+        if (s->stage[b]) cudaFreeHost(s->stage[b]);
     for (Request* r : s->queue) delete r;
     for (auto& kv : s->finished) delete kv.second;
     if (s->dtable) cudaFree(s->dtable);
@@ -362,15 +410,16 @@ int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
         if (req->size[d] <= 0 || req->size[d] > (1 << 20))
             return fail(LBM_ERR_INVALID_ARGUMENT, "size must be in [1, 2^20]");
     if (req->steps < 0) return fail(LBM_ERR_INVALID_ARGUMENT, "negative step count");
-    if (!(req->inv_tau > 0)) return fail(LBM_ERR_INVALID_ARGUMENT, "inv_tau must be positive");
-    if (population_bytes(req->size, s->cfg.storage) > s->arena_bytes ||
-        metadata_bytes(req->size) > (size_t)s->cfg.budget_bytes - s->arena_bytes)
+    if (!(req->inv_tau > 0) || !std::isfinite(req->inv_tau) || !std::isfinite(req->lid_velocity))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "inv_tau must be positive and finite");
+    if (population_bytes(req->size, s->cfg.storage) > s->arena_bytes)
         return fail(LBM_ERR_BUDGET, "request of %dx%dx%d cells can never fit the %lld-byte budget", req->size[0],
                     req->size[1], req->size[2], (long long)s->cfg.budget_bytes);
     Request* r = new (std::nothrow) Request();
     if (!r) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
     r->id = s->next_id++;
     r->spec = *req;
+    r->g = lbm::make_grid(req->size[0], req->size[1], req->size[2], elem_bytes(s->cfg.storage));
     r->submit_t = s->now();
     s->queue.push_back(r);
     if (id) *id = r->id;
@@ -383,68 +432,94 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     if (ran) *ran = 0;
     CK(cudaSetDevice(s->cfg.device), "cudaSetDevice");
     if (int rc = admit(s)) return rc;
-    // requests that need no steps finish at once
-    for (size_t i = 0; i < s->active.size();) {
-        if (s->active[i]->remaining == 0) {
-            Request* r = s->active[i];
-            s->active.erase(s->active.begin() + (long)i);
-            if (int rc = retire(s, r)) return rc;
-        } else {
-            ++i;
-        }
-    }
-    if (s->active.empty()) return LBM_OK;
+    std::vector<Request*> done;  // finish this round; their results are read before their memory is freed
+    take_finished(s, done);      // requests that need no steps finish at once
+    std::vector<Staged> now_staged;
+    // On a CUDA error every request taken off the active list completes with it.
+    auto abort_round = [&](int rc) {
+        for (const Staged& e : s->staged) complete(s, e.r, rc);
+        s->staged.clear();
+        for (Request* r : done) complete(s, r, rc);
+        return rc;
+    };
 
-    int64_t min_rem = s->active[0]->remaining;
-    long long cells = 0;
-    for (Request* r : s->active) {
-        min_rem = std::min(min_rem, r->remaining);
-        cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
-    }
     std::vector<Request*> run;
-    int64_t q;
-    if (min_rem == 1) {  // the last (alpha) step of the requests with one step left
-        for (Request* r : s->active)
-            if (r->remaining == 1) run.push_back(r);
-        q = 1;
-    } else {
-        run = s->active;
-        q = s->cfg.max_round_steps;
-        if (s->cfg.target_round_ms > 0 && s->rate > 0) {
-            const double want = s->cfg.target_round_ms * 1e-3 * s->rate / (double)cells;
-            q = std::min<int64_t>(q, std::max<int64_t>(2, (int64_t)want));
+    int64_t q = 0;
+    long long run_cells = 0, vblocks[2] = {0, 0};
+    if (!s->active.empty()) {
+        int64_t min_rem = s->active[0]->remaining;
+        long long cells = 0;
+        for (Request* r : s->active) {
+            min_rem = std::min(min_rem, r->remaining);
+            cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
         }
-        q = std::min<int64_t>(q, min_rem) & ~(int64_t)1;
-        if (q < 2) q = 2;
+        if (min_rem == 1) {  // the last (alpha) step of the requests with one step left
+            for (Request* r : s->active)
+                if (r->remaining == 1) run.push_back(r);
+            q = 1;
+        } else {
+            run = s->active;
+            q = s->cfg.max_round_steps;
+            if (s->cfg.target_round_ms > 0 && s->rate > 0) {
+                const double want = s->cfg.target_round_ms * 1e-3 * s->rate / (double)cells;
+                q = std::min<int64_t>(q, std::max<int64_t>(2, (int64_t)want));
+            }
+            q = std::min<int64_t>(q, min_rem) & ~(int64_t)1;
+            if (q < 2) q = 2;
+        }
+        for (Request* r : run) run_cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+        if (int rc = upload_table(s, run, vblocks)) return abort_round(rc);
     }
-    long long run_cells = 0;
-    for (Request* r : run) run_cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
-    long long vblocks[2] = {0, 0};
-    if (int rc = upload_table(s, run, vblocks)) return rc;
     const auto t_start = std::chrono::steady_clock::now();
     for (int64_t i = 0; i < q; ++i) {
         const int kind = (int)(i & 1);
         const lbm::BatchArgs a{s->arena, s->dtable, s->vb_map[kind], vblocks[kind], s->zero_word, (uint32_t)i};
-        CK(lbm::launch_batch_step(s->cfg.storage, s->variant, kind == 0, a, s->stream), "server step launch");
+        if (cudaError_t e = lbm::launch_batch_step(s->cfg.storage, s->variant, kind == 0, a, s->stream))
+            return abort_round(cuda_fail(e, "server step launch"));
     }
-    CK(cudaStreamSynchronize(s->stream), "server round");
-    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-    s->busy_s += dt;
-    s->rounds += 1;
-    s->lattice_updates += run_cells * q;
-    if (dt > 0 && q >= 2) s->rate = s->rate > 0 ? 0.7 * s->rate + 0.3 * (double)(run_cells * q) / dt
-                                                  : (double)(run_cells * q) / dt;
-    for (Request* r : run) r->remaining -= q;
-    for (size_t i = 0; i < s->active.size();) {
-        if (s->active[i]->remaining == 0) {
-            Request* r = s->active[i];
-            s->active.erase(s->active.begin() + (long)i);
-            if (int rc = retire(s, r)) return rc;
-        } else {
-            ++i;
+    for (Request* r : run)
+        if (r->remaining == q) done.push_back(r);
+    // this round's results queue behind its steps, into the buffer the host is not reading
+    const int b = s->cur;
+    size_t want = 0, largest = 0, next = 0;
+    for (const Request* r : done) {
+        want += round_up(result_bytes(r, s->cfg.storage));
+        largest = std::max(largest, round_up(result_bytes(r, s->cfg.storage)));
+    }
+    if (!done.empty()) {
+        if (int rc = reserve_stage(s, b, std::max(largest, std::min(want, kStageChunk)))) return abort_round(rc);
+        if (int rc = stage_results(s, b, done, 0, now_staged, next)) return abort_round(rc);
+    }
+    post_staged(s, b ^ 1, s->staged);  // the previous round's results, while the GPU runs
+    if (cudaError_t e = cudaStreamSynchronize(s->stream)) return abort_round(cuda_fail(e, "server round"));
+    if (!run.empty()) {
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        s->busy_s += dt;
+        s->rounds += 1;
+        s->lattice_updates += run_cells * q;
+        if (dt > 0 && q >= 2) s->rate = s->rate > 0 ? 0.7 * s->rate + 0.3 * (double)(run_cells * q) / dt
+                                                      : (double)(run_cells * q) / dt;
+        for (Request* r : run) r->remaining -= q;
+        std::vector<Request*> finished_now;
+        take_finished(s, finished_now);  // the requests of `done` that ran
+    }
+    s->staged = std::move(now_staged);
+    // results that did not fit the buffer: copy out what it holds, then the rest a buffer at a time
+    while (next < done.size()) {
+        post_staged(s, b, s->staged);
+        if (int rc = stage_results(s, b, done, next, s->staged, next)) {
+            done.assign(done.begin() + (long)(next), done.end());
+            return abort_round(rc);
+        }
+        if (cudaError_t e = cudaStreamSynchronize(s->stream)) {
+            done.assign(done.begin() + (long)(next), done.end());
+            return abort_round(cuda_fail(e, "server results"));
         }
     }
-    if (ran) *ran = 1;
+    for (Request* r : done) free_request(s, r);  // their results are read: the memory is free to admit
+    s->cur ^= 1;
+    if (s->active.empty()) post_staged(s, s->cur ^ 1, s->staged);  // no next round to overlap with
+    if (ran) *ran = run.empty() ? 0 : 1;
     return LBM_OK;
 }
 
@@ -481,7 +556,7 @@ int lbm_server_get_stats(const lbm_server* s, lbm_server_stats* st)
     st->queued = (int64_t)s->queue.size();
     st->active = (int64_t)s->active.size();
     st->completed = s->completed;
-    st->bytes_in_use = (int64_t)(s->alloc.used() + s->meta_in_use);
+    st->bytes_in_use = (int64_t)s->alloc.used();
     st->peak_bytes = (int64_t)s->peak_bytes;
     st->budget_bytes = s->cfg.budget_bytes;
     st->lattice_updates = s->lattice_updates;

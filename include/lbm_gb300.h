@@ -437,11 +437,12 @@ int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms
 /* ---- servers: cavity-solve requests with continuous batching ---------------
  * No counterpart in the reference.  Requests wait in FIFO order and are
  * admitted while their populations fit a device arena sized to 95 % of the
- * memory budget (the rest covers each request's flags and scratch).  Every
- * round advances all resident requests together (the batch kernel over a
- * packed table of them), sized to last about target_round_ms; finished
- * requests copy density and velocity to host memory, free their memory and
- * post a completion.  Requests that arrive while others run join the next
+ * memory budget (the rest covers the packed table and block maps); a request
+ * holds nothing on the device but its populations, since the walls and the
+ * lid come from the geometry.  Every round advances all resident requests
+ * together (the batch kernel over a packed table of them), sized to last
+ * about target_round_ms; finished requests write density and velocity to
+ * mapped host memory, free their memory and post a completion.  Requests that arrive while others run join the next
  * round as memory frees up.  Each request's fields are bit-identical to the
  * same cavity solved alone.  One host thread drives a server. */
 typedef struct lbm_server lbm_server;   /* opaque */

@@ -87,3 +87,26 @@ def test_late_short_request_overtakes_long_one(gpu):
                 fin[c["id"]] = c
         assert fin[b]["finish_time"] < fin[a]["finish_time"]
         assert fin[b]["admit_time"] < fin[a]["finish_time"]
+
+
+def test_results_beyond_one_staging_buffer(gpu):
+    """Six 256^3 FP32 requests that finish in the same round: their results
+    (1.6 GB) exceed one 1 GiB host staging buffer, so the last two are
+    written after the first four are copied out; all match solo runs."""
+    from cavityflow_cuda_gb300 import LbmServer
+
+    size, steps, nu = (256, 256, 256), 4, 0.02
+    lids = [0.01 * (i + 1) for i in range(6)]
+    inv = lattice_tau(nu, "f32")[1]
+    out = {}
+    with LbmServer(budget_bytes=12 << 30, storage="f32", max_round_steps=16, target_round_ms=0) as srv:
+        ids = {srv.submit(size, inv, float(np.float32(lid)), steps): i for i, lid in enumerate(lids)}
+        while len(out) < len(lids):
+            srv.round()
+            for c in srv.poll():
+                assert c["status"] == 0
+                out[ids[c["id"]]] = srv.take_result(c["id"])
+        assert srv.stats()["rounds"] == 1
+    for i in (0, 3, 4, 5):
+        rho, u = _solo(size, nu, lids[i], steps, "f32")
+        assert np.array_equal(out[i][0], rho) and np.array_equal(out[i][1], u), i
