@@ -10,8 +10,9 @@
 //      the lid come from the geometry, so a request has no flag array);
 //   2. advances every resident request by the same even number of steps with
 //      the batch kernel over a packed table of the resident domains (sized so
-//      the round lasts about the target time), or, when some request has a
-//      single step left, runs that last alpha step for those requests alone;
+//      the round lasts about the target time); requests with a single (alpha)
+//      step left sit at the end of the table and take it in the round's first
+//      launch, which the later launches stop short of;
 //   3. retires finished requests: one kernel per request writes density and
 //      velocity of the last collided time level straight into mapped pinned
 //      host memory, one stream synchronisation covers them all, then the
@@ -443,42 +444,56 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
         return rc;
     };
 
-    std::vector<Request*> run;
+    // `run` = the requests advanced q (even) steps, then the `tail`: requests
+    // with one (alpha) step left, which take it in the round's first launch
+    // only.  Every request has taken an even number of steps before, so the
+    // first launch is alpha for all of them; the later launches stop at the
+    // tail's first virtual block.
+    std::vector<Request*> run, tail;
     int64_t q = 0;
-    long long run_cells = 0, vblocks[2] = {0, 0};
+    long long run_cells = 0, tail_cells = 0, vblocks[2] = {0, 0}, vb_run[2] = {0, 0};
     if (!s->active.empty()) {
-        int64_t min_rem = s->active[0]->remaining;
-        long long cells = 0;
+        int64_t min_rem = -1;
         for (Request* r : s->active) {
-            min_rem = std::min(min_rem, r->remaining);
-            cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+            const long long c = (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+            if (r->remaining == 1) {
+                tail.push_back(r);
+                tail_cells += c;
+            } else {
+                run.push_back(r);
+                run_cells += c;
+                min_rem = min_rem < 0 ? r->remaining : std::min(min_rem, r->remaining);
+            }
         }
-        if (min_rem == 1) {  // the last (alpha) step of the requests with one step left
-            for (Request* r : s->active)
-                if (r->remaining == 1) run.push_back(r);
-            q = 1;
-        } else {
-            run = s->active;
+        if (!run.empty()) {
             q = s->cfg.max_round_steps;
             if (s->cfg.target_round_ms > 0 && s->rate > 0) {
-                const double want = s->cfg.target_round_ms * 1e-3 * s->rate / (double)cells;
+                const double want = s->cfg.target_round_ms * 1e-3 * s->rate / (double)(run_cells + tail_cells);
                 q = std::min<int64_t>(q, std::max<int64_t>(2, (int64_t)want));
             }
             q = std::min<int64_t>(q, min_rem) & ~(int64_t)1;
             if (q < 2) q = 2;
+        } else {
+            q = 1;
         }
-        for (Request* r : run) run_cells += (long long)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+        const size_t n_run = run.size();
+        run.insert(run.end(), tail.begin(), tail.end());
         if (int rc = upload_table(s, run, vblocks)) return abort_round(rc);
+        for (int kind = 0; kind < 2; ++kind)
+            vb_run[kind] = tail.empty() ? vblocks[kind] : s->table[n_run].block_start[kind];
+        run.resize(n_run);
     }
     const auto t_start = std::chrono::steady_clock::now();
     for (int64_t i = 0; i < q; ++i) {
         const int kind = (int)(i & 1);
-        const lbm::BatchArgs a{s->arena, s->dtable, s->vb_map[kind], vblocks[kind], s->zero_word, (uint32_t)i};
+        const long long n = i == 0 ? vblocks[kind] : vb_run[kind];
+        const lbm::BatchArgs a{s->arena, s->dtable, s->vb_map[kind], n, s->zero_word, (uint32_t)i};
         if (cudaError_t e = lbm::launch_batch_step(s->cfg.storage, s->variant, kind == 0, a, s->stream))
             return abort_round(cuda_fail(e, "server step launch"));
     }
     for (Request* r : run)
         if (r->remaining == q) done.push_back(r);
+    done.insert(done.end(), tail.begin(), tail.end());
     // this round's results queue behind its steps, into the buffer the host is not reading
     const int b = s->cur;
     size_t want = 0, largest = 0, next = 0;
@@ -492,14 +507,16 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     }
     post_staged(s, b ^ 1, s->staged);  // the previous round's results, while the GPU runs
     if (cudaError_t e = cudaStreamSynchronize(s->stream)) return abort_round(cuda_fail(e, "server round"));
-    if (!run.empty()) {
+    if (q > 0) {
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        const long long updates = run.empty() ? tail_cells : run_cells * q + tail_cells;
         s->busy_s += dt;
         s->rounds += 1;
-        s->lattice_updates += run_cells * q;
-        if (dt > 0 && q >= 2) s->rate = s->rate > 0 ? 0.7 * s->rate + 0.3 * (double)(run_cells * q) / dt
-                                                      : (double)(run_cells * q) / dt;
+        s->lattice_updates += updates;
+        if (dt > 0 && q >= 2) s->rate = s->rate > 0 ? 0.7 * s->rate + 0.3 * (double)updates / dt
+                                                      : (double)updates / dt;
         for (Request* r : run) r->remaining -= q;
+        for (Request* r : tail) r->remaining -= 1;
         std::vector<Request*> finished_now;
         take_finished(s, finished_now);  // the requests of `done` that ran
     }
@@ -519,7 +536,7 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     for (Request* r : done) free_request(s, r);  // their results are read: the memory is free to admit
     s->cur ^= 1;
     if (s->active.empty()) post_staged(s, s->cur ^ 1, s->staged);  // no next round to overlap with
-    if (ran) *ran = run.empty() ? 0 : 1;
+    if (ran) *ran = q > 0 ? 1 : 0;
     return LBM_OK;
 }
 
