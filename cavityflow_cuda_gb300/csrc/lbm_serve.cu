@@ -183,6 +183,18 @@ void free_request(lbm_server* s, Request* r)
     }
 }
 
+void complete(lbm_server* s, Request* r, int status)
+{
+    r->status = status;
+    free_request(s, r);
+    r->finish_t = s->now();
+    if (status == LBM_OK) s->completed += 1;
+    s->finished[r->id] = r;
+    const int64_t cells = (int64_t)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
+    s->completions.push_back(
+        {r->id, r->spec.steps, status == LBM_OK ? cells : 0, status, 0, r->submit_t, r->admit_t, r->finish_t});
+}
+
 int admit(lbm_server* s)
 {
     while (!s->queue.empty()) {
@@ -194,7 +206,11 @@ int admit(lbm_server* s)
         r->offset = off;
         r->bytes = bytes;
         // populations at rest; the steps that follow on the same stream see them
-        CK(lbm::launch_init_populations(s->cfg.storage, s->arena + off, r->g, s->stream), "server init launch");
+        if (cudaError_t e = lbm::launch_init_populations(s->cfg.storage, s->arena + off, r->g, s->stream)) {
+            const int rc = cuda_fail(e, "server init launch");
+            complete(s, r, rc);
+            return rc;
+        }
         r->admit_t = s->now();
         r->remaining = r->spec.steps;
         s->active.push_back(r);
@@ -294,18 +310,6 @@ int stage_results(lbm_server* s, int b, const std::vector<Request*>& done, size_
         used += bytes;
     }
     return LBM_OK;
-}
-
-void complete(lbm_server* s, Request* r, int status)
-{
-    r->status = status;
-    free_request(s, r);
-    r->finish_t = s->now();
-    if (status == LBM_OK) s->completed += 1;
-    s->finished[r->id] = r;
-    const int64_t cells = (int64_t)r->spec.size[0] * r->spec.size[1] * r->spec.size[2];
-    s->completions.push_back(
-        {r->id, r->spec.steps, status == LBM_OK ? cells : 0, status, 0, r->submit_t, r->admit_t, r->finish_t});
 }
 
 // Copies results whose kernels have completed out of staging buffer b and
