@@ -489,7 +489,10 @@ int lbm_server_create(const lbm_server_config* config, lbm_server** out);
 int lbm_server_destroy(lbm_server* server);
 /* Queues a request; LBM_ERR_BUDGET if it could never fit the budget. */
 int lbm_server_submit(lbm_server* server, const lbm_request* request, int64_t* id);
-/* Admits, runs one round and retires; *ran = 0 when nothing was resident. */
+/* Admits, runs one round and retires; *ran = 0 when nothing was resident.
+ * A request that finishes in a round is posted (lbm_server_poll) during the
+ * next round, whose GPU work hides the copy of its result, or at the end of
+ * the same round when no request is left running. */
 int lbm_server_round(lbm_server* server, int32_t* ran);
 /* Moves up to `capacity` new completions to `out`. */
 int lbm_server_poll(lbm_server* server, lbm_completion* out, int32_t capacity, int32_t* count);
