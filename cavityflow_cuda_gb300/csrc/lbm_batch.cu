@@ -167,7 +167,8 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     size_t elems = 0;
     b->table.resize((size_t)count);
     for (int i = 0; i < count; ++i) {
-        const lbm::Grid g = lbm::make_grid(domains[i].size[0], domains[i].size[1], domains[i].size[2], eb);
+        const lbm::Grid g =
+            lbm::make_grid(domains[i].size[0], domains[i].size[1], domains[i].size[2], eb, lbm::kPackedX1Align);
         offsets[(size_t)i] = elems;
         elems += (size_t)lbm::Q * g.S;  // S keeps every slot 256-byte aligned
         lbm::BatchDomain& d = b->table[(size_t)i];
@@ -202,7 +203,8 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
         p.device = device;
         p.fast_variant = b->variant + 1;
         lbm_solver* v = nullptr;
-        int r = create_solver(&p, static_cast<char*>(b->pool) + offsets[(size_t)i] * (size_t)eb, &v);
+        int r = create_solver(&p, static_cast<char*>(b->pool) + offsets[(size_t)i] * (size_t)eb, &v,
+                              lbm::kPackedX1Align);
         if (r) return bail(r);
         v->batch = b;
         b->views.push_back(v);

@@ -421,7 +421,7 @@ int lbm_create(const lbm_params* prm, lbm_solver** out)
 
 }  // extern "C"
 
-int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out)
+int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out, int x1_align)
 {
     if (!prm || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
@@ -451,7 +451,7 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
     if (!s) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->storage = prm->storage;
     s->device = prm->device;
-    s->g = lbm::make_grid(prm->size[0], prm->size[1], prm->size[2], elem_bytes(prm->storage));
+    s->g = lbm::make_grid(prm->size[0], prm->size[1], prm->size[2], elem_bytes(prm->storage), x1_align);
     s->p.inv_tau = prm->inv_tau;
     s->p.lid_u = prm->lid_velocity;
     s->p.gx = prm->gravity[0];
@@ -558,6 +558,7 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
+    info->x1_column = s->g.xoff + 1;
     return LBM_OK;
 }
 

@@ -60,6 +60,14 @@ __host__ __device__ constexpr T weight(int k)
 // 32 consecutive groups start on a sector.  P leaves room for one scalar
 // access right of the last group and is a multiple of 32 bytes, and every
 // slot starts on a 256-byte boundary.
+//
+// Batches and servers pack their boxes' rows tighter (x1_align = 16): x = 1
+// on a 16-byte boundary and P a multiple of 16 bytes.  L2 fetches a 128-byte
+// line whole when a short row touches part of it; with packed rows the
+// neighbouring rows' cells fill more of those lines.  The register kernels
+// only need x = 1 on a 16-byte boundary and index through idx(), so both
+// layouts run the same code with the same results; the bulk-copy kernels run
+// on the default layout only.
 // ---------------------------------------------------------------------------
 struct Grid {
     int nx, ny, nz;      // interior cells
@@ -83,12 +91,12 @@ struct Grid {
     __host__ __device__ long long cells() const { return (long long)(nx + 2) * (ny + 2) * (nz + 2); }
 };
 
-inline Grid make_grid(int nx, int ny, int nz, int elem_bytes)
+inline Grid make_grid(int nx, int ny, int nz, int elem_bytes, int x1_align = 32)
 {
     Grid g;
     g.nx = nx; g.ny = ny; g.nz = nz;
     g.V = 16 / elem_bytes;
-    const int sector = 32 / elem_bytes;
+    const int sector = (x1_align == 16 ? 16 : 32) / elem_bytes;
     g.xoff = sector - 1;
     g.G = (nx + g.V - 1) / g.V;
     const long long need = (long long)g.xoff + (long long)g.G * g.V + 2;  // last scalar column + 1
@@ -98,6 +106,12 @@ inline Grid make_grid(int nx, int ny, int nz, int elem_bytes)
     g.S = (g.PY * (nz + 2) + slot_align - 1) / slot_align * slot_align;
     return g;
 }
+
+// Alignment of x = 1 in the rows of batch and server boxes (see above).
+constexpr int kPackedX1Align = 16;
+
+// True for the default layout (x = 1 on a 32-byte boundary).
+inline bool default_layout(const Grid& g, int elem_bytes) { return g.xoff == 32 / elem_bytes - 1; }
 
 // ---------------------------------------------------------------------------
 // Storage types.  F64/F32 hold f_i; F16S/BF16S/F16SR hold the deviation

@@ -49,7 +49,9 @@ int default_variant(int storage);
 int default_batch_variant(int storage);
 // Creates a solver; with `external_dd` its populations live there (a batch
 // pool) and are initialised but never freed by the solver.
-int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out);
+// x1_align: 32 (the default layout) or 16 (the packed rows of batch pools,
+// see make_grid).
+int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out, int x1_align = 32);
 void destroy_solver(lbm_solver* s);
 int* err_flag(lbm_solver* s);
 // Two device words of the solver: [0] the first step of a graph replay,

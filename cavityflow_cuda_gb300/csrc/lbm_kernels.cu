@@ -442,6 +442,7 @@ bool fast_variant_fits(int storage, int variant, const Grid& g)
     if (variant < kRegisterVariants) return true;
     const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
     const int elem = storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 ? 4 : 2;
+    if (!default_layout(g, elem)) return false;  // the bulk-copy kernels run on the default layout only
     int dev = 0, max_optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     if (cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;

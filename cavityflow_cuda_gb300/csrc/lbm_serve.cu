@@ -162,9 +162,15 @@ struct lbm_server {
 
 namespace {
 
+// A request's layout: the packed rows of batch pools.
+lbm::Grid request_grid(const int32_t size[3], int storage)
+{
+    return lbm::make_grid(size[0], size[1], size[2], elem_bytes(storage), lbm::kPackedX1Align);
+}
+
 size_t population_bytes(const int32_t size[3], int storage)
 {
-    const lbm::Grid g = lbm::make_grid(size[0], size[1], size[2], elem_bytes(storage));
+    const lbm::Grid g = request_grid(size, storage);
     return ((size_t)lbm::Q * g.S * elem_bytes(storage) + kAlign - 1) / kAlign * kAlign;
 }
 
@@ -424,7 +430,7 @@ int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
     if (!r) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
     r->id = s->next_id++;
     r->spec = *req;
-    r->g = lbm::make_grid(req->size[0], req->size[1], req->size[2], elem_bytes(s->cfg.storage));
+    r->g = request_grid(req->size, s->cfg.storage);
     r->submit_t = s->now();
     s->queue.push_back(r);
     if (id) *id = r->id;

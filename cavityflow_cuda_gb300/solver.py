@@ -74,7 +74,7 @@ class _Info(C.Structure):
                 ("block_threads", C.c_int32), ("beta_cells_per_thread", C.c_int32),
                 ("beta_block_threads", C.c_int32), ("beta_block_exchange", C.c_int32),
                 ("fused_multiply_add", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
-                ("device_bytes", C.c_int64)]
+                ("device_bytes", C.c_int64), ("x1_column", C.c_int64)]
 
 
 def declared_functions() -> list[str]:

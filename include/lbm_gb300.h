@@ -210,6 +210,9 @@ typedef struct lbm_info {
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */
+    int64_t x1_column;          /* column of interior cell x = 1 in a row: 32
+                                   bytes in (the default), or 16 for the
+                                   packed rows of batch domains               */
 } lbm_info;
 
 /* ---- lifecycle ------------------------------------------------------------ */

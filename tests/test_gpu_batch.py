@@ -63,3 +63,29 @@ def test_batch_views_getters_and_guards(gpu):
         with pytest.raises(LbmError):
             b.run(2)
         assert b._lib.lbm_destroy(v._h) == 1   # a batch domain is freed with its batch
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16sr", "f64"])
+def test_batch_packed_rows(gpu, storage):
+    """Batch domains pack their rows (x = 1 on a 16-byte boundary, 16-byte
+    row pitch) while a single solver keeps the default 32-byte layout; the
+    results are the same bit for bit."""
+    from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmBatch
+    from cavityflow_cuda_gb300.workloads import lattice_tau
+
+    T = np.float64 if storage == "f64" else np.float32
+    sizes = [(12, 9, 7), (20, 11, 5), (30, 6, 9), (7, 13, 10), (40, 5, 6), (3, 4, 5)]
+    doms = [(size, lattice_tau(0.02 + 0.01 * i, storage)[1], float(T(0.05 + 0.01 * i)))
+            for i, size in enumerate(sizes)]
+    elem = {"f32": 4, "f16sr": 2, "f64": 8}[storage]
+    with LbmBatch(doms, storage=storage) as b:
+        b.run(33)
+        views = [b.domain(i) for i in range(len(doms))]
+        assert all(v.info()["x1_column"] * elem == 16 for v in views)
+        assert all(v.info()["row_pitch"] * elem % 16 == 0 for v in views)
+        got = [v.get_all() for v in views]
+    for i, (size, inv_tau, lid) in enumerate(doms):
+        with CLbmSolverGB300(size, inv_tau, lid, storage=storage) as s:
+            assert s.info()["x1_column"] * elem == 32
+            s.run(33)
+            assert np.array_equal(got[i].view(np.uint8), s.get_all().view(np.uint8)), (storage, size)
