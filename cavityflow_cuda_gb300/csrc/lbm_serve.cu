@@ -446,20 +446,25 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     std::vector<Request*> done;  // finish this round; their results are read before their memory is freed
     take_finished(s, done);      // requests that need no steps finish at once
     std::vector<Staged> now_staged;
-    // On a CUDA error every request taken off the active list completes with it.
-    auto abort_round = [&](int rc) {
-        for (const Staged& e : s->staged) complete(s, e.r, rc);
-        s->staged.clear();
-        for (Request* r : done) complete(s, r, rc);
-        return rc;
-    };
-
     // `run` = the requests advanced q (even) steps, then the `tail`: requests
     // with one (alpha) step left, which take it in the round's first launch
     // only.  Every request has taken an even number of steps before, so the
     // first launch is alpha for all of them; the later launches stop at the
     // tail's first virtual block.
     std::vector<Request*> run, tail;
+    // On a CUDA error every request of the round, and every result not yet
+    // posted, completes with the error and leaves the active list.
+    auto abort_round = [&](int rc) {
+        for (const Staged& e : s->staged) complete(s, e.r, rc);
+        s->staged.clear();
+        for (const std::vector<Request*>* list : {&done, &run, &tail})
+            for (Request* r : *list)
+                if (r->finish_t < 0) complete(s, r, rc);
+        s->active.erase(std::remove_if(s->active.begin(), s->active.end(),
+                                       [](const Request* r) { return r->finish_t >= 0; }),
+                        s->active.end());
+        return rc;
+    };
     int64_t q = 0;
     long long run_cells = 0, tail_cells = 0, vblocks[2] = {0, 0}, vb_run[2] = {0, 0};
     if (!s->active.empty()) {
@@ -534,14 +539,8 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     // results that did not fit the buffer: copy out what it holds, then the rest a buffer at a time
     while (next < done.size()) {
         post_staged(s, b, s->staged);
-        if (int rc = stage_results(s, b, done, next, s->staged, next)) {
-            done.assign(done.begin() + (long)(next), done.end());
-            return abort_round(rc);
-        }
-        if (cudaError_t e = cudaStreamSynchronize(s->stream)) {
-            done.assign(done.begin() + (long)(next), done.end());
-            return abort_round(cuda_fail(e, "server results"));
-        }
+        if (int rc = stage_results(s, b, done, next, s->staged, next)) return abort_round(rc);
+        if (cudaError_t e = cudaStreamSynchronize(s->stream)) return abort_round(cuda_fail(e, "server results"));
     }
     for (Request* r : done) free_request(s, r);  // their results are read: the memory is free to admit
     s->cur ^= 1;
