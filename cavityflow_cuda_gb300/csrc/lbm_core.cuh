@@ -266,10 +266,14 @@ struct FastDiv {
         }
         return f;
     }
-    __device__ __forceinline__ uint32_t div(uint32_t n) const
+    __host__ __device__ __forceinline__ uint32_t div(uint32_t n) const
     {
         if (l == 0) return n;
+#ifdef __CUDA_ARCH__
         const uint32_t t = __umulhi(n, m);
+#else
+        const uint32_t t = (uint32_t)(((uint64_t)n * m) >> 32);  // the same high word, for host checks
+#endif
         return (t + ((n - t) >> 1)) >> (l - 1);
     }
 };
