@@ -700,7 +700,7 @@ inline long long set_batch_shape(BatchDomain& d, int kind, int cpt, int block)
 
 // The group of thread t of a domain's virtual blocks, t = ((z-1) * ny +
 // (y-1)) * G + gi; threads past the last group get a valid group, inactive.
-__device__ __forceinline__ Cells cells_of_vblock(const BatchDomain& d, int which, uint32_t t)
+__host__ __device__ __forceinline__ Cells cells_of_vblock(const BatchDomain& d, int which, uint32_t t)
 {
     const FastDiv& dg = d.div_g[which];
     const uint32_t row = dg.div(t);
