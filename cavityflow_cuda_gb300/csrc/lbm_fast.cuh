@@ -121,7 +121,8 @@ struct Cells {
 
 // From an index i over the G * ny groups of plane z (the step kernels' grid:
 // x over a plane's groups, y over planes); divG divides by G.
-__device__ __forceinline__ Cells cells_of_plane(const Grid& g, int G, const FastDiv& divG, uint32_t i, int z)
+__host__ __device__ __forceinline__ Cells cells_of_plane(const Grid& g, int G, const FastDiv& divG, uint32_t i,
+                                                     int z)
 {
     Cells c;
     c.active = i < (uint32_t)G * (uint32_t)g.ny;
