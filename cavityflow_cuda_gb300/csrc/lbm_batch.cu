@@ -7,6 +7,7 @@
 // apply unchanged.  A batch step is one launch of the persistent batch
 // kernel (lbm_fast.cuh) over the packed domain table; long runs replay a CUDA
 // graph of captured alpha/beta pairs.
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -145,10 +146,13 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     *out = nullptr;
     if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
-    for (int i = 0; i < count; ++i)
+    for (int i = 0; i < count; ++i) {
         for (int d = 0; d < 3; ++d)
             if (domains[i].size[d] <= 0 || domains[i].size[d] > (1 << 20))
                 return fail(LBM_ERR_INVALID_ARGUMENT, "domain %d: size must be in [1, 2^20]", i);
+        if (!(domains[i].inv_tau > 0) || !std::isfinite(domains[i].inv_tau) || !std::isfinite(domains[i].lid_velocity))
+            return fail(LBM_ERR_INVALID_ARGUMENT, "domain %d: inv_tau must be positive and finite", i);
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LBM_ERR_NO_DEVICE, "no CUDA device visible");
     if (device < 0 || device >= ndev) return fail(LBM_ERR_INVALID_ARGUMENT, "device %d not in [0,%d)", device, ndev);

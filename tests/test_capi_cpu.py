@@ -121,3 +121,31 @@ def test_launch_variant_menu_size(lib):
     parity tests enumerate exactly these."""
     assert lib.lbm_fast_variant_count() == 24
     assert lib.lbm_register_variant_count() == 18
+
+
+def test_batch_and_server_arguments_checked_before_the_device(lib):
+    """Batches and servers reject bad arguments before any CUDA call, with
+    LBM_ERR_INVALID_ARGUMENT (1); valid ones reach the device check."""
+    import math
+
+    import torch
+
+    from cavityflow_cuda_gb300 import LbmBatch, LbmError, LbmServer
+
+    good = [((8, 8, 8), 1.6, 0.05), ((5, 6, 7), 1.2, 0.02)]
+    for bad in ([((8, 0, 8), 1.6, 0.05)], [((8, 8, 8), 0.0, 0.05)], [((8, 8, 8), math.inf, 0.05)],
+                [((8, 8, 8), 1.6, math.nan)], [((8, 8, (1 << 20) + 1), 1.6, 0.05)]):
+        with pytest.raises(LbmError) as ei:
+            LbmBatch(good + bad, storage="f32")
+        assert ei.value.status == 1, bad
+    for kw in (dict(budget_bytes=1 << 19), dict(budget_bytes=1 << 30, max_round_steps=1)):
+        with pytest.raises(LbmError) as ei:
+            LbmServer(storage="f32", **kw)
+        assert ei.value.status == 1, kw
+    if not torch.cuda.is_available():
+        with pytest.raises(LbmError) as ei:
+            LbmBatch(good, storage="f16sr")
+        assert ei.value.status == 10
+        with pytest.raises(LbmError) as ei:
+            LbmServer(budget_bytes=1 << 30, storage="f16s")
+        assert ei.value.status == 10
