@@ -149,3 +149,26 @@ def test_batch_and_server_arguments_checked_before_the_device(lib):
         with pytest.raises(LbmError) as ei:
             LbmServer(budget_bytes=1 << 30, storage="f16s")
         assert ei.value.status == 10
+
+
+@pytest.mark.parametrize("kw,status", [
+    (dict(size=(0, 8, 8)), 1),
+    (dict(size=(8, 8, (1 << 20) + 1)), 1),
+    (dict(boundary=(1, 1, 1, 1, 16, 1)), 1),
+    (dict(inv_tau=0.0), 1),
+    (dict(inv_tau=float("nan")), 1),
+    (dict(inv_tau=float("inf")), 1),
+    (dict(lid_velocity=float("nan")), 1),
+    (dict(storage="f16s", gravity=(0.0, -1e-5, 0.0)), 5),   # gravity: F64 and F32 only
+    (dict(storage="f32", fused_multiply_add=True), 1),      # fused multiply-adds: F64 only
+])
+def test_create_argument_checks_before_the_device(lib, kw, status):
+    """lbm_create rejects bad parameters with a status code (the reference
+    asserts or exits) before any CUDA call, so these hold without a GPU."""
+    from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmError
+
+    args = dict(size=(8, 8, 8), inv_tau=1.6, lid_velocity=0.05, storage="f32")
+    args.update(kw)
+    with pytest.raises(LbmError) as ei:
+        CLbmSolverGB300(args.pop("size"), args.pop("inv_tau"), args.pop("lid_velocity"), **args)
+    assert ei.value.status == status, kw
