@@ -71,8 +71,8 @@ def parse():
                     help="register variant of --workload batch (default: autotuned per storage)")
     ap.add_argument("--precision-size", type=int, default=512)
     ap.add_argument("--precision-steps", type=int, default=5000)
-    ap.add_argument("--serve-count", type=int, default=1000)
-    ap.add_argument("--serve-step-scale", type=float, default=0.05)
+    ap.add_argument("--serve-count", type=int, default=10000)
+    ap.add_argument("--serve-step-scale", type=float, default=0.01)
     return ap.parse_args()
 
 
@@ -94,13 +94,13 @@ def config_dict(a, world):
 # CPU legs (oracle as the checker/baseline only)
 # ---------------------------------------------------------------------------
 
-def cpu_run(a, seconds_target, steps_max=None, use_reference=True):
+def cpu_run(a, seconds_target, steps_max=None, use_reference=True, threads=None):
     """Time the reference algorithm on host cores over z-slabs of the domain.
 
     Uses the reference's own CPU kernels (oracle/_ref) where they were built
-    (only possible where the reference checkout exists), else the C port
-    (oracle/liblbm_oracle.so) with OpenMP over all cores.  Returns
-    (mlups, cores, kind, sample)."""
+    for this host and load (the reference runs them on one thread), else the C
+    port (oracle/liblbm_oracle.so) with OpenMP over `threads` threads (default:
+    all cores).  Returns (mlups, cores, kind, sample)."""
     from oracle import oracle as orc
 
     dtype = np.float64 if a.storage == "f64" else np.float32
@@ -109,11 +109,12 @@ def cpu_run(a, seconds_target, steps_max=None, use_reference=True):
     if use_reference and os.path.exists(orc.REF_SO):
         try:
             lib, kind = orc.Reference(), "reference"
-        except OSError:
+        except OSError:  # built for another host architecture
             lib = None
     if lib is None:
         orc.build()
         lib = orc.Oracle()
+        lib.set_num_threads(threads if threads else os.cpu_count() or 1)
     cores = lib.num_threads() if kind == "port" else 1
     n = a.size
     _, itau = orc.tau_of(a.nu, dtype)
@@ -140,6 +141,17 @@ def cpu_run(a, seconds_target, steps_max=None, use_reference=True):
     sample = (f"{steps} steps over a {n}x{n}x{planes} interior slab of the {n}^3 domain "
               f"({n * n * planes * steps / 1e6:.1f} M lattice updates, {dt:.1f} s)")
     return mlups, cores, kind, sample
+
+
+def cpu_baseline(a):
+    """The reference CPU path as the reference runs it (one thread: its
+    kernels are not parallelised), and the C port over every host core."""
+    one, cores1, kind1, sample1 = cpu_run(a, a.cpu_seconds / 3, use_reference=True, threads=1)
+    allc, cores, kind, sample = cpu_run(a, a.cpu_seconds, use_reference=False)
+    return {"value": round(one, 3), "unit": "MLUPS", "cores": cores1, "kind": kind1,
+            "sample": sample1 + "; 1 core used, the reference CPU kernels' own parallelism",
+            "nproc": os.cpu_count(),
+            "all_cores": {"value": round(allc, 3), "unit": "MLUPS", "cores": cores, "kind": kind, "sample": sample}}
 
 
 def reference_arm(a):
@@ -301,10 +313,13 @@ def profile_traffic(a, kernel):
     return e["dram_bytes_per_launch"] * (a.size ** 3) / float(e["cells"])
 
 
-def batch_measure(storage, count, steps, device=0, variant=-1):
+def batch_measure(storage, count, steps, device=0, variant=-1, ref_fields=None):
     """Aggregate MLUPS of the seeded batch of box cavities (512 edges in
     [16,96], lid in [0.02,0.1], Re log-uniform in [10,2000], seed 0), all
-    advanced together; CUDA events around `steps` steps on one stream."""
+    advanced together; CUDA events around `steps` steps on one stream.  With
+    `ref_fields` (velocities of the same batch run in FP64 for the same 4 +
+    `steps` steps, batch_fields) the relative L2 and max velocity error of this
+    storage against FP64 over every domain's interior."""
     import torch
 
     from cavityflow_cuda_gb300 import LbmBatch
@@ -327,11 +342,44 @@ def batch_measure(storage, count, steps, device=0, variant=-1):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         info = b.info()
+        err = velocity_error(batch_fields(b), ref_fields) if ref_fields is not None else None
     lups = float(info["interior_cells"]) * steps
-    return {"storage": storage, "domains": count, "steps": steps, "interior_cells": info["interior_cells"],
-            "mlups": round(lups / (ms / 1e3) / 1e6, 1), "ms": round(ms, 2), "variant": tuned[0],
-            "variant_ms_per_pair": [round(v, 4) for v in tuned[1]],
-            "device_gb": round(info["device_bytes"] / 1e9, 3)}
+    out = {"storage": storage, "domains": count, "steps": steps, "interior_cells": info["interior_cells"],
+           "mlups": round(lups / (ms / 1e3) / 1e6, 1), "ms": round(ms, 2), "variant": tuned[0],
+           "variant_ms_per_pair": [round(v, 4) for v in tuned[1]],
+           "device_gb": round(info["device_bytes"] / 1e9, 3)}
+    if err is not None:
+        out["l2_err_vs_f64"], out["max_abs_err_vs_f64"] = err
+    return out
+
+
+def batch_fields(b):
+    """Velocity of every domain of a batch (float64 copies)."""
+    return [b.domain(i).getVelocities().astype(np.float64) for i in range(len(b))]
+
+
+def batch_reference_fields(count, steps, device=0):
+    """The seeded batch run in FP64 for `steps` steps; its velocity fields."""
+    from cavityflow_cuda_gb300 import LbmBatch
+    from cavityflow_cuda_gb300.workloads import batch_workload
+
+    cav = batch_workload(count=count, seed=0)
+    with LbmBatch([c.solver_args("f64") for c in cav], storage="f64", device=device) as b:
+        b.run(steps)
+        return batch_fields(b)
+
+
+def velocity_error(fields, ref):
+    """Relative L2 norm of the velocity difference over all fields, and the
+    largest absolute difference."""
+    num = den = 0.0
+    worst = 0.0
+    for f, r in zip(fields, ref):
+        d = f - r
+        num += float((d * d).sum())
+        den += float((r * r).sum())
+        worst = max(worst, float(np.abs(d).max()))
+    return (float(np.sqrt(num / den)) if den > 0 else 0.0), worst
 
 
 def single_measure(storage, n, steps, device=0):
@@ -354,10 +402,12 @@ def single_measure(storage, n, steps, device=0):
     return float(n) ** 3 * steps / (ms / 1e3) / 1e6
 
 
-def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
+def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0, fp64_fma=True):
     """L2 and max velocity error of FP32, FP16-shifted and BF16-shifted storage
     against an FP64 run of this solver (same cavity), the FP64 mass drift, and
-    each storage's MLUPS (CUDA events around the run)."""
+    each storage's MLUPS (CUDA events around the run).  fp64_fma: the FP64 run
+    uses the fused multiply-add kernels (1.4x faster; within 1e-15 of the
+    unfused FP64 over 1000 steps, far below the errors measured here)."""
     import torch
 
     from cavityflow_cuda_gb300 import CLbmSolverGB300
@@ -369,7 +419,9 @@ def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
         _, inv_tau = lattice_tau(nu, storage)
         T = np.float64 if storage == "f64" else np.float32
         stream = torch.cuda.Stream()
-        with CLbmSolverGB300((n, n, n), inv_tau, float(T(lid)), storage=storage, device=device) as s:
+        fma = fp64_fma and storage == "f64"
+        with CLbmSolverGB300((n, n, n), inv_tau, float(T(lid)), storage=storage, device=device,
+                             fused_multiply_add=fma) as s:
             m0 = s.reduce()[0]
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -387,21 +439,29 @@ def precision_measure(n, steps, nu=0.0512, lid=0.1, device=0):
         d = fields[storage] - ref
         res[storage]["l2_err_vs_f64"] = float(np.sqrt((d ** 2).sum()) / norm)
         res[storage]["max_abs_err_vs_f64"] = float(np.abs(d).max())
+    res["f64"]["fused_multiply_add"] = bool(fp64_fma)
     res["f16s_speedup_vs_f32"] = round(res["f16s"]["mlups"] / res["f32"]["mlups"], 3)
     res["f16sr_speedup_vs_f32"] = round(res["f16sr"]["mlups"] / res["f32"]["mlups"], 3)
     return res
 
 
-def serve_measure(storage, count, step_scale, budget_gb=150.0, rate=200.0, seed=1, target_ms=50, device=0):
+def serve_measure(storage, count, step_scale, budget_gb=150.0, rate=200.0, seed=1, target_ms=50, device=0,
+                  l2_sample=0, l2_max_edge=64):
     """p50/p99 latency and aggregate MLUPS of the seeded request stream (cube
     edges {32..256} weighted, steps uniform in [500, 20000] times step_scale,
     lid 0.05, Re log-uniform in [10, 5000], Poisson arrivals), replayed in
-    real time against a server with a budget_gb HBM budget."""
+    real time against a server with a budget_gb HBM budget.  l2_sample > 0:
+    the results of the first l2_sample requests with edges up to l2_max_edge
+    are kept and compared with the same cavities solved alone in FP64
+    (relative L2 velocity error over the sample)."""
     from cavityflow_cuda_gb300 import LbmServer
     from cavityflow_cuda_gb300.workloads import serving_workload
 
     reqs = serving_workload(count=count, seed=seed, rate=rate)
     steps = [max(2, int(round(r.steps * step_scale))) for r in reqs]
+    sample = [i for i in range(count) if reqs[i].size[0] <= l2_max_edge][:l2_sample]
+    sampled = set(sample)
+    kept = {}
     lat, wait, lups = [], [], 0
     with LbmServer(budget_bytes=int(budget_gb * 1e9), storage=storage, device=device, target_round_ms=target_ms,
                    max_round_steps=512) as srv:
@@ -422,45 +482,108 @@ def serve_measure(storage, count, step_scale, budget_gb=150.0, rate=200.0, seed=
                 wait.append(c["admit_time"] - c["submit_time"])
                 lups += c["cells"] * c["steps"]
                 last_finish = max(last_finish, hsub[c["id"]] + (c["finish_time"] - c["submit_time"]))
-                srv.take_result(c["id"], copy=False)
+                if k in sampled:
+                    kept[k] = srv.take_result(c["id"], copy=True)[1].astype(np.float64)
+                else:
+                    srv.take_result(c["id"], copy=False)
                 done += 1
             if not ran and i < count:
                 time.sleep(max(0.0, min(0.005, reqs[i].arrival - (time.perf_counter() - t0))))
         st = srv.stats()
     span = last_finish - reqs[0].arrival
     lat = np.array(lat)
-    return {"storage": storage, "requests": count, "step_scale": step_scale, "arrival_rate": rate,
+    err = None
+    if kept:
+        from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+        ref = []
+        for k in sample:
+            size, inv_tau, lid_u = reqs[k].solver_args("f64")
+            with CLbmSolverGB300(size, inv_tau, lid_u, storage="f64", device=device) as s:
+                s.run(steps[k])
+                ref.append(s.getVelocities().astype(np.float64))
+        err = velocity_error([kept[k] for k in sample], ref)
+    out = {"storage": storage, "requests": count, "step_scale": step_scale, "arrival_rate": rate,
             "budget_gb": budget_gb, "p50_latency_s": round(float(np.percentile(lat, 50)), 3),
             "p99_latency_s": round(float(np.percentile(lat, 99)), 3),
             "p50_queue_wait_s": round(float(np.percentile(wait, 50)), 3),
             "aggregate_mlups": round(lups / span / 1e6, 1), "busy_mlups": round(st["lattice_updates"] /
                                                                                st["busy_seconds"] / 1e6, 1),
             "makespan_s": round(span, 2), "rounds": st["rounds"], "peak_gb": round(st["peak_bytes"] / 1e9, 2)}
+    if err is not None:
+        out["l2_err_vs_f64"], out["max_abs_err_vs_f64"] = err
+        out["l2_sample"] = f"{len(sample)} requests (edges <= {l2_max_edge}), each solved alone in FP64"
+    return out
+
+
+def moving_wall_measure(n=384, steps=200, device=0):
+    """The mass-conserving moving-wall lid beside the reference's injection
+    lid: FP32 MLUPS of each at n^3 (lid 0.05, nu 0.0192; CUDA events around
+    `steps` graph-replayed steps), and the relative FP64 mass change of each
+    over 1000 steps of the 64^3 cavity (lid 0.05, nu 0.032, Re 100)."""
+    import torch
+
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+    from cavityflow_cuda_gb300.workloads import lattice_tau
+
+    out = {"domain": [n] * 3, "steps": steps}
+    _, itau = lattice_tau(0.0192, "f32")
+    for mode in ("injection", "wall"):
+        stream = torch.cuda.Stream()
+        with CLbmSolverGB300((n, n, n), itau, 0.05, storage="f32", device=device, lid=mode) as s:
+            s.run(8, stream=stream)
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run(steps, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+        out[f"{mode}_f32_mlups"] = round(float(n) ** 3 * steps / (ms / 1e3) / 1e6, 1)
+        _, itau64 = lattice_tau(0.032, "f64")
+        with CLbmSolverGB300((64, 64, 64), itau64, 0.05, storage="f64", device=device, lid=mode) as s:
+            m0 = s.reduce()[0]
+            s.run(1000)
+            out[f"{mode}_f64_mass_change_rel_64cubed_1000_steps"] = float((s.reduce()[0] - m0) / m0)
+    return out
 
 
 def extensions(a):
-    """Bounded measurements of the batch and precision extensions, attached to
-    the benchmark line (full-size runs: --workload batch|precision)."""
+    """The extension measurements at their stated configurations, attached to
+    the benchmark line: precision (512^3, lid 0.1, nu 0.0512, 5000 steps, every
+    storage against an FP64 run), the moving-wall lid beside the injection
+    lid, the 512-cavity batch in FP32/F16S/F16SR with each 16-bit result's
+    error against an FP64 batch, and the 10,000-request serving stream (steps
+    scaled by --serve-step-scale) in FP32 and F16SR with the error of a sample
+    against FP64 solves."""
     out = {}
     try:
-        out["batch_f32"] = batch_measure("f32", a.batch_count, 2000)
-        out["batch_f16s"] = batch_measure("f16s", a.batch_count, 2000)
-        out["batch_f16sr"] = batch_measure("f16sr", a.batch_count, 2000)
-        out["batch_note"] = "batched MLUPS over the seeded 512-cavity workload; compare with single-domain MLUPS"
+        out["precision"] = precision_measure(a.precision_size, a.precision_steps)
+        out["precision_note"] = (f"{a.precision_size}^3, {a.precision_steps} steps, lid 0.1, nu 0.0512 (Re 1000); "
+                                 "errors against the FP64 run of this solver")
     except Exception as e:  # keep the main line whatever happens here
+        out["precision_error"] = repr(e)
+    try:
+        out["moving_wall"] = moving_wall_measure()
+    except Exception as e:
+        out["moving_wall_error"] = repr(e)
+    try:
+        ref = batch_reference_fields(a.batch_count, 4 + a.batch_steps)
+        for st in ("f32", "f16s", "f16sr"):
+            out[f"batch_{st}"] = batch_measure(st, a.batch_count, a.batch_steps, ref_fields=ref)
+        del ref
+        out["batch_note"] = (f"batched MLUPS over the seeded {a.batch_count}-cavity workload, {a.batch_steps} "
+                             "steps; velocity errors against the same batch in FP64; compare with "
+                             "single-domain MLUPS")
+    except Exception as e:
         out["batch_error"] = repr(e)
     try:
-        out["serve_f32"] = serve_measure("f32", 200, 0.02)
-        out["serve_note"] = ("first 200 requests of the seeded 10,000-request stream, steps scaled by 0.02; "
-                             "--workload serve runs larger samples")
+        for st in ("f32", "f16sr"):
+            out[f"serve_{st}"] = serve_measure(st, a.serve_count, a.serve_step_scale, l2_sample=16)
+        out["serve_note"] = (f"the seeded {a.serve_count}-request stream at 200 req/s, steps U[500,20000] scaled "
+                             f"by {a.serve_step_scale}, 150 GB budget")
     except Exception as e:
         out["serve_error"] = repr(e)
-    try:
-        out["precision"] = precision_measure(256, 1000)
-        out["precision_note"] = ("256^3, 1000 steps, lid 0.1, nu 0.0512 (the 512^3 / 5000-step configuration's "
-                                 "physics on a smaller grid; --workload precision runs the full size)")
-    except Exception as e:
-        out["precision_error"] = repr(e)
     return out
 
 
@@ -616,8 +739,7 @@ def run_gpu(a):
 
     cpu = None
     if rank == 0 and not a.no_cpu:
-        mlups, cores, kind, sample = cpu_run(a, a.cpu_seconds, use_reference=False)
-        cpu = {"value": round(mlups, 3), "unit": "MLUPS", "cores": cores, "kind": kind, "sample": sample}
+        cpu = cpu_baseline(a)
 
     ext = extensions(a) if (rank == 0 and world == 1 and not a.no_extensions) else None
 

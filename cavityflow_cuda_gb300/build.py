@@ -9,8 +9,9 @@ beside it (host/lbm_main.cpp).  Object files go to
 The library is compiled with ``-fmad=false``: the FP64/FP32 collision must
 not be contracted into fused multiply-adds, so that it performs the same IEEE
 operations as the reference kernels.  The one exception is ``*_fma.cu``
-(``fast_f64_fma.cu``): the opt-in FP64 kernels whose multiply-adds are fused
-on purpose (lbm_params.fused_multiply_add).
+(``fast_fma.cu``): the opt-in FP64 and FP32 kernels whose multiply-adds are
+fused on purpose (lbm_params.fused_multiply_add), built like the reference's
+own nvcc build (-fmad=true -ftz=true).
 """
 from __future__ import annotations
 
@@ -66,8 +67,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
         # .cpp units include the kernel headers, so they are compiled as CUDA too
         lang = ["-x", "cu"] if src.endswith(".cpp") else []
         flags = NVCC_FLAGS
-        if src.endswith("_fma.cu"):  # FP64 kernels that fuse multiply-adds on purpose (fast_f64_fma.cu)
-            flags = [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS]
+        if src.endswith("_fma.cu"):  # kernels that fuse multiply-adds on purpose (fast_fma.cu), as
+            # the reference's -use_fast_math build does (which also flushes FP32 subnormals)
+            flags = [("-fmad=true" if f == "-fmad=false" else f) for f in NVCC_FLAGS] + ["-ftz=true"]
         cmd = [nvcc, *ARCH, *flags, *lang, "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)

@@ -106,9 +106,9 @@ int lbm_detail::default_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F32: return 13;
-    case LBM_STORAGE_F16S: return 15;
-    case LBM_STORAGE_BF16S: return 11;
-    case LBM_STORAGE_F16SR: return 15;
+    case LBM_STORAGE_F16S: return 18;
+    case LBM_STORAGE_BF16S: return 18;
+    case LBM_STORAGE_F16SR: return 18;
     default: return 3;
     }
 }
@@ -193,11 +193,13 @@ int refresh_path(lbm_solver* s)
     return LBM_OK;
 }
 
-// Storage code of the vectorised step kernels: FP64 with fused multiply-adds
-// has its own kernel family (lbm::kStorageF64Fma).
+// Storage code of the vectorised step kernels: FP64 and FP32 with fused
+// multiply-adds have kernel families of their own (lbm::kStorageF64Fma,
+// lbm::kStorageF32Fma).
 int kernel_storage(const lbm_solver* s)
 {
-    return s->fma && s->storage == LBM_STORAGE_F64 ? lbm::kStorageF64Fma : s->storage;
+    if (!s->fma) return s->storage;
+    return s->storage == LBM_STORAGE_F64 ? lbm::kStorageF64Fma : lbm::kStorageF32Fma;
 }
 
 int step(lbm_solver* s, bool alpha, const int32_t* origin, const int32_t* size, cudaStream_t st)
@@ -437,10 +439,14 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
         return fail(LBM_ERR_UNSUPPORTED, "gravity is supported with F64 and F32 storage only");
     if (prm->fused_multiply_add != 0 && prm->fused_multiply_add != 1)
         return fail(LBM_ERR_INVALID_ARGUMENT, "fused_multiply_add must be 0 or 1");
-    if (prm->fused_multiply_add && prm->storage != LBM_STORAGE_F64)
-        return fail(LBM_ERR_INVALID_ARGUMENT, "fused_multiply_add applies to F64 storage only");
+    if (prm->fused_multiply_add && prm->storage != LBM_STORAGE_F64 && prm->storage != LBM_STORAGE_F32)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "fused_multiply_add applies to F64 and F32 storage only");
     if (!(prm->inv_tau > 0) || !std::isfinite(prm->inv_tau) || !std::isfinite(prm->lid_velocity))
         return fail(LBM_ERR_INVALID_ARGUMENT, "inv_tau must be positive and finite");
+    if (prm->lid_mode != LBM_LID_INJECTION && prm->lid_mode != LBM_LID_MOVING_WALL)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "lid_mode must be LBM_LID_INJECTION or LBM_LID_MOVING_WALL");
+    if (prm->lid_mode == LBM_LID_MOVING_WALL && prm->boundary[3] != LBM_OBSTACLE)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "a moving-wall lid needs an OBSTACLE top face (boundary[3])");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(LBM_ERR_NO_DEVICE, "no CUDA device visible");
@@ -465,6 +471,7 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
     }
     s->variant = prm->fast_variant == 0 ? default_variant(s->storage) : prm->fast_variant - 1;
     s->fma = prm->fused_multiply_add == 1;
+    s->lid_mode = prm->lid_mode;
 
     auto bail = [&](int r) { destroy_solver(s); return r; };
     cudaError_t e = cudaSetDevice(s->device);
@@ -552,12 +559,15 @@ int lbm_get_info(const lbm_solver* s, lbm_info* info)
                             info->beta_block_threads);
     info->fused_multiply_add = s->fma ? 1 : 0;
     info->beta_block_exchange = s->variant >= lbm::kRegisterVariants ? 0
+                                : lbm::kFastMenu[s->variant].packed != 0 && elem_bytes(s->storage) == 2 ? 3
                                 : lbm::kFastMenu[s->variant].direct       ? 2
                                 : lbm::kFastMenu[s->variant].block_exchange ? 1
                                                                             : 0;
     info->row_pitch = s->g.P;
     info->slot_stride = s->g.S;
     info->device_bytes = s->device_bytes;
+    info->lid_mode = s->lid_mode;
+    info->moving_wall = s->p.wall_y > 0 ? 1 : 0;
     info->x1_column = s->g.xoff + 1;
     return LBM_OK;
 }
@@ -580,6 +590,12 @@ int lbm_value_size(const lbm_solver* s)
 int lbm_set_driven_cavity(lbm_solver* s)
 {
     if (int r = check_solver(s)) return r;
+    if (s->lid_mode == LBM_LID_MOVING_WALL) {
+        // the top wall starts moving; captured graphs hold the old parameters
+        s->p.wall_y = s->g.ny;
+        drop_graph(s);
+        return LBM_OK;
+    }
     const int32_t origin[3] = {1, s->g.ny, 1};   // src/CController.cpp:1313
     const int32_t size[3] = {s->g.nx, 1, s->g.nz};
     std::vector<int32_t> lid((size_t)s->g.nx * s->g.nz, LBM_VELOCITY_INJECTION);

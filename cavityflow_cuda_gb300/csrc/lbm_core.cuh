@@ -131,7 +131,7 @@ struct F64 {
     static constexpr int kStepLog2 = 0;
 };
 // FP64 whose step kernels are compiled with fused multiply-adds
-// (fast_f64_fma.cu, the one translation unit built with -fmad=true); a type of
+// (fast_fma.cu, the one translation unit built with -fmad=true); a type of
 // its own so that its kernel instantiations never merge with F64's.
 struct F64F : F64 {};
 struct F32 {
@@ -144,6 +144,9 @@ struct F32 {
     __device__ static T load_step(bits b) { return load(b); }
     static constexpr int kStepLog2 = 0;
 };
+// FP32 whose step kernels fuse multiply-adds (fast_fma.cu), for the same
+// reason as F64F.
+struct F32F : F32 {};
 struct F16S {
     using bits = unsigned short;
     using T = float;
@@ -281,12 +284,15 @@ struct FastDiv {
 // Scalar lattice parameters of one domain, and the time step of the next
 // launch, *step_base + step_off (it keys stochastic rounding; step_base points
 // to device memory so that captured graphs can be replayed at later steps).
+// wall_y: the row of cells under a moving top wall (the opt-in
+// mass-conserving lid, see wall_correct), or 0 when the top wall is at rest.
 struct Params {
     double inv_tau;
     double lid_u;
     double gx, gy, gz;
     const uint32_t* step_base = nullptr;
     uint32_t step_off = 0;
+    int wall_y = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -480,6 +486,31 @@ template <typename T>
 __device__ __forceinline__ void inject(T* f, T rho0, T lid_u)
 {
     equilibrium(rho0, lid_u, T(0), T(0), f);
+}
+
+// Moving top wall: the opt-in alternative to the reference's injection lid
+// (no reference counterpart).  The top face y = ny + 1 is an obstacle wall
+// moving at U along x, and the cells of row y = ny stay FLUID.  Walls bounce
+// populations back (A-A: a population that entered a wall slot is read back
+// reversed), so populations 5 (-x-y) and 6 (+x-y) that such a cell reads are
+// populations 4 (+x+y) and 7 (-x+y) returned by the wall.  Ladd's moving-wall
+// rule, f_opp(i) = f_i - 6 w_i rho_w (c_i . U) with rho_w = 1, adds
+// -6 (1/36) U = -U/6 to population 5 and +U/6 to population 6.  The two
+// corrections of a cell cancel, so the total mass stays constant.  `du` is
+// U/6 in a storage type's step units (wall_shift).
+template <class St>
+__device__ __forceinline__ typename St::T wall_shift(typename St::T lid_u)
+{
+    using T = typename St::T;
+    T du = lid_u * (T(1) / T(6));
+    if constexpr (St::kStepLog2 != 0) du *= (float)(1u << St::kStepLog2);
+    return du;
+}
+template <typename T>
+__device__ __forceinline__ void wall_correct(T* f, T du)
+{
+    f[5] -= du;
+    f[6] += du;
 }
 
 // The same in a storage type's step units (scaled deviations for F16SR).

@@ -20,7 +20,10 @@
 //                  edges use scalar accesses.
 //   beta_fast_direct -- the same step with no exchange at all: each thread
 //                  reads and writes its own one-cell-shifted windows with
-//                  element-aligned pieces (the default for FP32 and FP16).
+//                  element-aligned pieces (the default for FP32).
+//   beta_fast_pk -- the direct windows for 16-bit storage with two cells'
+//                  populations packed per 32-bit word and paired conversions
+//                  (the default for the 16-bit storages).
 //   batch_step  -- the persistent kernel of a batch of cavities, running the
 //                  same per-thread bodies over a packed domain table.
 //
@@ -138,7 +141,8 @@ __host__ __device__ __forceinline__ Cells cells_of_plane(const Grid& g, int G, c
 template <class St, int CPT>
 __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                             const typename St::T inv_tau, const typename St::T lid_u,
-                                            const int lid_y, const Cells c, const uint32_t step)
+                                            const int lid_y, const int wall_y, const Cells c,
+                                            const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -153,6 +157,8 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
     for (int k = 0; k < Q; ++k) IO::load_raw(dd + k * g.S + base, f[k]);
 
     const bool lid = (y == lid_y);
+    const bool wall = (y == wall_y);
+    const T du = wall_shift<St>(lid_u);
     const T rho0 = St::shifted ? T(0) : T(1);
     const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
@@ -161,6 +167,7 @@ __device__ __forceinline__ void alpha_cells(typename St::bits* __restrict__ dd, 
         T c[Q];
 #pragma unroll
         for (int k = 0; k < Q; ++k) c[k] = St::load_step(f[k][v]);
+        if (wall) wall_correct(c, du);
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
@@ -176,12 +183,13 @@ template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                           const typename St::T inv_tau,
                                                           const typename St::T lid_u, const int lid_y,
+                                                          const int wall_y,
                                                           const uint32_t* __restrict__ step_base,
                                                           const uint32_t step_off, const FastDiv divG,
                                                           const int z_base)
 {
     const int G = (g.nx + CPT - 1) / CPT;
-    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+    alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y,
                          cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
                          step_of<St>(step_base, step_off));
 }
@@ -192,7 +200,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) alpha_fast(typename St::bits* __r
 template <class St, int CPT>
 __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, const Grid& g,
                                            const typename St::T inv_tau, const typename St::T lid_u,
-                                           const int lid_y, const Cells c, const uint32_t step)
+                                           const int lid_y, const int wall_y, const Cells c,
+                                           const uint32_t step)
 {
     using T = typename St::T;
     using IO = Vio<St, CPT>;
@@ -246,6 +255,8 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
     });
 
     const bool lid = (y == lid_y);
+    const bool wall = (y == wall_y);
+    const T du = wall_shift<St>(lid_u);
     const T rho0 = St::shifted ? T(0) : T(1);
     const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
@@ -254,6 +265,7 @@ __device__ __forceinline__ void beta_cells(typename St::bits* __restrict__ dd, c
         T c[Q];
 #pragma unroll
         for (int k = 0; k < Q; ++k) c[opp(k)] = St::load_step(p[k][v]);
+        if (wall) wall_correct(c, du);
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
@@ -352,7 +364,8 @@ struct Window {
 template <class St, int CPT>
 __device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict__ dd, const Grid& g,
                                                   const typename St::T inv_tau, const typename St::T lid_u,
-                                                  const int lid_y, const Cells c, const uint32_t step)
+                                                  const int lid_y, const int wall_y, const Cells c,
+                                                  const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -373,6 +386,8 @@ __device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict_
     });
 
     const bool lid = (y == lid_y);
+    const bool wall = (y == wall_y);
+    const T du = wall_shift<St>(lid_u);
     const T rho0 = St::shifted ? T(0) : T(1);
     const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
@@ -381,6 +396,7 @@ __device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict_
         T cc[Q];
 #pragma unroll
         for (int k = 0; k < Q; ++k) cc[opp(k)] = St::load_step(p[k][v]);
+        if (wall) wall_correct(cc, du);
         if (lid) inject_step<St>(cc, rho0, lid_u);
         else collide<St>(cc, inv_tau);
         uint32_t h = 0;
@@ -398,16 +414,227 @@ __device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict_
     });
 }
 
+// ---------------------------------------------------------------------------
+// Beta step for 16-bit storage with two cells' populations per 32-bit word.
+//
+// The direct windows above keep each 16-bit population in a register of its
+// own, convert it on its own and assemble the vectors element by element.
+// Here a slot's CPT cells stay packed as the words that the slot's memory
+// pieces load and store -- for a slot with c_x = 0 the pairs (0,1), (2,3) of
+// its aligned vector, for c_x = +-1 the window's single first cell, its
+// 4-byte pairs (1,2), ... and its single last cell (PkSlot) -- so no element
+// is moved between registers: inputs are half selections of the words, and
+// each pair of results is rounded and packed by one paired conversion
+// (cvt.rz.f16x2.f32 after the stochastic-rounding dither, cvt.rn.f16x2 /
+// cvt.rn.bf16x2 otherwise).  A cell's first result of a pair waits as a float
+// (`pend`) until its partner is collided.  The results are bit-identical to
+// the per-cell conversions (the same roundings), with half the registers for
+// the populations (96 registers at 4 cells per thread against 128) and fewer
+// instructions.
+//
+// Loads (kVecLoads): the window's pieces (2-, 4- and 2-byte accesses for 4
+// cells), or the aligned vector that holds all but one of the window's
+// elements plus that one element (2 accesses; the extra bytes come from the
+// same L1 sectors).  Stores always use the window's pieces, since the aligned
+// vector's other element belongs to the neighbouring group.  Rows whose last
+// group is partial take beta_cells_direct for that group.
+// ---------------------------------------------------------------------------
+constexpr int kPkMaxWords = 5;
+
+// Where cell v's 16-bit value sits in the packed words of a slot with shift S
+// (its stored form: the window's pieces).
+template <int CPT, int S>
+struct PkSlot {
+    __host__ __device__ static constexpr int word(int v) { return S == 0 ? v >> 1 : (v == 0 ? 0 : (v + 1) >> 1); }
+    __host__ __device__ static constexpr int half(int v) { return S == 0 ? (v & 1) : (v == 0 ? 0 : ((v + 1) & 1)); }
+    // a 2-byte piece: converted alone
+    __host__ __device__ static constexpr bool single(int v) { return S != 0 && (v == 0 || v == CPT - 1); }
+    // the first cell of a 4-byte pair: waits for its partner
+    __host__ __device__ static constexpr bool first(int v) { return !single(v) && half(v) == 0; }
+    // with vector loads, where cell v's value sits as loaded
+    __host__ __device__ static constexpr int in_word(int v, bool vec)
+    {
+        return !vec || S == 0 ? word(v) : S > 0 ? (v == CPT - 1 ? CPT / 2 : (v + 1) >> 1) : (v == 0 ? 0 : 1 + ((v - 1) >> 1));
+    }
+    __host__ __device__ static constexpr int in_half(int v, bool vec)
+    {
+        return !vec || S == 0 ? half(v) : S > 0 ? (v == CPT - 1 ? 0 : (v + 1) & 1) : (v == 0 ? 0 : (v - 1) & 1);
+    }
+};
+
+// The window [S, S + CPT) of a slot (elements relative to the cells' aligned
+// vector) as its widest naturally aligned pieces, each moved whole into or out
+// of the packed words.
+template <int CPT, int S, int E>
+struct PkPiece {
+    static constexpr int kEnd = S + CPT;
+    static constexpr int width()
+    {
+        int w = 1;
+        while (2 * w * 2 <= 16 && E % (2 * w) == 0 && E + 2 * w <= kEnd) w *= 2;
+        return w;
+    }
+    static constexpr int W = width();
+    static constexpr int w0 = PkSlot<CPT, S>::word(E - S);
+    __device__ static void load(const unsigned short* p, uint32_t (&w)[kPkMaxWords])
+    {
+        if constexpr (W == 1) w[w0] = (uint32_t)p[E];
+        else if constexpr (W == 2) w[w0] = *reinterpret_cast<const uint32_t*>(p + E);
+        else if constexpr (W == 4) {
+            const uint2 t = *reinterpret_cast<const uint2*>(p + E);
+            w[w0] = t.x; w[w0 + 1] = t.y;
+        } else {
+            const uint4 t = *reinterpret_cast<const uint4*>(p + E);
+            w[w0] = t.x; w[w0 + 1] = t.y; w[w0 + 2] = t.z; w[w0 + 3] = t.w;
+        }
+        if constexpr (E + W < kEnd) PkPiece<CPT, S, E + W>::load(p, w);
+    }
+    __device__ static void store(unsigned short* p, const uint32_t (&w)[kPkMaxWords])
+    {
+        if constexpr (W == 1) p[E] = (unsigned short)w[w0];
+        else if constexpr (W == 2) *reinterpret_cast<uint32_t*>(p + E) = w[w0];
+        else if constexpr (W == 4) *reinterpret_cast<uint2*>(p + E) = make_uint2(w[w0], w[w0 + 1]);
+        else *reinterpret_cast<uint4*>(p + E) = make_uint4(w[w0], w[w0 + 1], w[w0 + 2], w[w0 + 3]);
+        if constexpr (E + W < kEnd) PkPiece<CPT, S, E + W>::store(p, w);
+    }
+};
+
+// Loads of a slot with shift S: the pieces, or (kVec, S != 0) the aligned
+// vector (words 0.. for S > 0, 1.. for S < 0) and the one element outside it
+// (word CPT/2 for S > 0, word 0 for S < 0), as PkSlot::in_word describes.
+template <int CPT, int S, bool kVec>
+__device__ __forceinline__ void pk_load(const unsigned short* p, uint32_t (&w)[kPkMaxWords])
+{
+    if constexpr (S == 0 || !kVec) {
+        PkPiece<CPT, S, S>::load(p, w);
+    } else {
+        constexpr int o = S > 0 ? 0 : 1;
+        if constexpr (CPT == 4) {
+            const uint2 t = *reinterpret_cast<const uint2*>(p);
+            w[o] = t.x; w[o + 1] = t.y;
+        } else {
+            const uint4 t = *reinterpret_cast<const uint4*>(p);
+            w[o] = t.x; w[o + 1] = t.y; w[o + 2] = t.z; w[o + 3] = t.w;
+        }
+        if constexpr (S > 0) w[CPT / 2] = (uint32_t)p[CPT];
+        else w[0] = (uint32_t)p[-1];
+    }
+}
+
+// A 16-bit pattern (low or high half of a word) in the step's arithmetic type.
+template <class St>
+__device__ __forceinline__ float pk_in(uint32_t w, int hi)
+{
+    if constexpr (std::is_same<St, BF16S>::value) return __uint_as_float(hi ? (w & 0xffff0000u) : (w << 16));
+    else return __half2float(__ushort_as_half((unsigned short)(hi ? (w >> 16) : (w & 0xffffu))));
+}
+
+// Step results rounded to 16-bit patterns: one alone, or two packed (lo, hi)
+// by one paired conversion with the same rounding as the single one.
+template <class St>
+__device__ __forceinline__ uint32_t pk_one(float v, uint32_t h, int k)
+{
+    return (uint32_t)store_pop<St>(v, h, k);
+}
+template <class St>
+__device__ __forceinline__ uint32_t pk_two(float lo, float hi, uint32_t hlo, uint32_t hhi, int k)
+{
+    uint32_t r;
+    if constexpr (St::stochastic) {
+        const float a = __uint_as_float(__float_as_uint(hi) + sr_dither(hhi, k));
+        const float b = __uint_as_float(__float_as_uint(lo) + sr_dither(hlo, k));
+        asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a), "f"(b));
+    } else if constexpr (std::is_same<St, BF16S>::value) {
+        asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    } else {
+        asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    }
+    return r;
+}
+
+template <class St, int CPT, bool kVec>
+__device__ __forceinline__ void beta_cells_pk(typename St::bits* __restrict__ dd, const Grid& g,
+                                              const typename St::T inv_tau, const typename St::T lid_u,
+                                              const int lid_y, const int wall_y, const Cells c,
+                                              const uint32_t step)
+{
+    static_assert(sizeof(typename St::bits) == 2, "16-bit storage only");
+    if (!c.active) return;
+    const int gi = c.gi, y = c.y, z = c.z;
+    const int x0 = 1 + gi * CPT;
+    if (x0 + CPT - 1 > g.nx) {  // the row's last, partial group
+        beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, step);
+        return;
+    }
+    const long long base = g.idx(x0, y, z);
+    uint32_t w[Q][kPkMaxWords];
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
+        pk_load<CPT, dir_x(k), kVec>(dd + rb, w[k]);
+    });
+    const bool lid = (y == lid_y);
+    const bool wall = (y == wall_y);
+    const float du = wall_shift<St>(lid_u);
+    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
+    float pend[Q];
+    uint32_t hprev = 0;
+    static_for<0, CPT>([&](auto vc) {
+        constexpr int v = decltype(vc)::value;
+        float cc[Q];
+        static_for<0, Q>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            using P = PkSlot<CPT, dir_x(k)>;
+            cc[opp(k)] = pk_in<St>(w[k][P::in_word(v, kVec)], P::in_half(v, kVec));
+        });
+        if (wall) wall_correct(cc, du);
+        if (lid) inject_step<St>(cc, 0.0f, lid_u);
+        else collide<St>(cc, inv_tau);
+        uint32_t h = 0;
+        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
+        static_for<0, Q>([&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            using P = PkSlot<CPT, dir_x(k)>;
+            if constexpr (P::single(v)) w[k][P::word(v)] = pk_one<St>(cc[k], h, k);
+            else if constexpr (P::first(v)) pend[k] = cc[k];
+            else w[k][P::word(v)] = pk_two<St>(pend[k], cc[k], hprev, h, k);
+        });
+        hprev = h;
+    });
+    static_for<0, Q>([&](auto kc) {
+        constexpr int k = decltype(kc)::value;
+        constexpr int cx = dir_x(k);
+        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
+        PkPiece<CPT, cx, cx>::store(dd + rb, w[k]);
+    });
+}
+
+template <class St, int CPT, int BLOCK, int MINB, bool kVec>
+__global__ void __launch_bounds__(BLOCK, MINB) beta_fast_pk(typename St::bits* __restrict__ dd, const Grid g,
+                                                            const typename St::T inv_tau,
+                                                            const typename St::T lid_u, const int lid_y,
+                                                            const int wall_y,
+                                                            const uint32_t* __restrict__ step_base,
+                                                            const uint32_t step_off, const FastDiv divG,
+                                                            const int z_base)
+{
+    const int G = (g.nx + CPT - 1) / CPT;
+    beta_cells_pk<St, CPT, kVec>(dd, g, inv_tau, lid_u, lid_y, wall_y,
+                                 cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
+                                 step_of<St>(step_base, step_off));
+}
+
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_direct(typename St::bits* __restrict__ dd, const Grid g,
                                                                 const typename St::T inv_tau,
                                                                 const typename St::T lid_u, const int lid_y,
+                                                                const int wall_y,
                                                                 const uint32_t* __restrict__ step_base,
                                                                 const uint32_t step_off, const FastDiv divG,
                                                                 const int z_base)
 {
     const int G = (g.nx + CPT - 1) / CPT;
-    beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+    beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y,
                                cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
                                step_of<St>(step_base, step_off));
 }
@@ -421,7 +648,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_direct(typename St::bit
 template <class St, int CPT, int BLOCK>
 __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ dd, const Grid& g,
                                                const typename St::T inv_tau, const typename St::T lid_u,
-                                               const int lid_y, const Cells c, const uint32_t step)
+                                               const int lid_y, const int wall_y, const Cells c,
+                                               const uint32_t step)
 {
     using T = typename St::T;
     using bits = typename St::bits;
@@ -498,6 +726,8 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
     });
 
     const bool lid = (y == lid_y);
+    const bool wall = (y == wall_y);
+    const T du = wall_shift<St>(lid_u);
     const T rho0 = St::shifted ? T(0) : T(1);
     const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
 #pragma unroll
@@ -506,6 +736,7 @@ __device__ __forceinline__ void beta_cells_blk(typename St::bits* __restrict__ d
         T c[Q];
 #pragma unroll
         for (int k = 0; k < Q; ++k) c[opp(k)] = St::load_step(p[k][v]);
+        if (wall) wall_correct(c, du);
         if (lid) inject_step<St>(c, rho0, lid_u);
         else collide<St>(c, inv_tau);
         uint32_t h = 0;
@@ -572,13 +803,14 @@ template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_blk(typename St::bits* __restrict__ dd, const Grid g,
                                                              const typename St::T inv_tau,
                                                              const typename St::T lid_u, const int lid_y,
+                                                             const int wall_y,
                                                              const uint32_t* __restrict__ step_base,
                                                              const uint32_t step_off, const FastDiv divG,
                                                              const int z_base)
 {
     const int G = (g.nx + CPT - 1) / CPT;
     beta_cells_blk<St, CPT, BLOCK>(
-        dd, g, inv_tau, lid_u, lid_y,
+        dd, g, inv_tau, lid_u, lid_y, wall_y,
         cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
         step_of<St>(step_base, step_off));
 }
@@ -587,12 +819,13 @@ template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast(typename St::bits* __restrict__ dd, const Grid g,
                                                          const typename St::T inv_tau,
                                                          const typename St::T lid_u, const int lid_y,
+                                                         const int wall_y,
                                                          const uint32_t* __restrict__ step_base,
                                                          const uint32_t step_off, const FastDiv divG,
                                                          const int z_base)
 {
     const int G = (g.nx + CPT - 1) / CPT;
-    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y,
+    beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y,
                         cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
                         step_of<St>(step_base, step_off));
 }
@@ -622,8 +855,8 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
         const unsigned bx = (unsigned)((per_plane + block - 1) / block);
         for (int z0 = 0; z0 < g.nz; z0 += kMaxPlanes) {
             const int planes = g.nz - z0 < kMaxPlanes ? g.nz - z0 : kMaxPlanes;
-            kern<<<dim3(bx, (unsigned)planes), block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.step_base,
-                                                               p.step_off, divG, z0);
+            kern<<<dim3(bx, (unsigned)planes), block, 0, st>>>(d, g, T(p.inv_tau), T(p.lid_u), lid_y, p.wall_y,
+                                                               p.step_base, p.step_off, divG, z0);
             if (z0 > 0) add_launches(1);
         }
         return cudaGetLastError();
@@ -635,7 +868,9 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
     }
     constexpr KernelShape k = fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    if constexpr (fv.direct) return launch(beta_fast_direct<St, CPT, k.block, k.minb>, CPT, k.block);
+    if constexpr (fv.packed != 0 && sizeof(typename St::bits) == 2)
+        return launch(beta_fast_pk<St, CPT, k.block, k.minb, fv.packed == 2>, CPT, k.block);
+    else if constexpr (fv.direct) return launch(beta_fast_direct<St, CPT, k.block, k.minb>, CPT, k.block);
     else if constexpr (fv.block_exchange) return launch(beta_fast_blk<St, CPT, k.block, k.minb>, CPT, k.block);
     else return launch(beta_fast<St, CPT, k.block, k.minb>, CPT, k.block);
 }
@@ -678,6 +913,7 @@ struct alignas(16) BatchDomain {
     double lid_u;
     int lid_y;
     uint32_t step0;            // added to the launch's step: this domain's own step count
+    int wall_y;                // row under a moving top wall, 0: none (see wall_correct)
     long long block_start[2];  // first virtual block of this domain: [0] alpha, [1] beta kernel
     FastDiv div_g[2];          // division by the groups per row of the alpha / beta shape
     FastDiv div_ny;            // division by ny
@@ -733,7 +969,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Every thread of a CTA walks the same virtual blocks, so that barrier and
 // the block-wide barriers of the exchanging beta body are reached uniformly.
 // kBeta: 0 warp exchange (beta_cells), 1 block exchange (beta_cells_blk),
-// 2 direct windows (beta_cells_direct).
+// 2 direct windows (beta_cells_direct), 3 and 4 packed 16-bit windows
+// (beta_cells_pk with piece or vector loads).
 template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, int kBeta>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
                                                           const BatchDomain* __restrict__ doms,
@@ -770,11 +1007,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         const Grid g = d.g;  // in registers for the body (its barriers would force shared-memory reloads)
         typename St::bits* const dd = pool + d.offset;
         const T inv_tau = T(d.inv_tau), lid_u = T(d.lid_u);
-        const int lid_y = d.lid_y;
-        if constexpr (kAlpha) alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
-        else if constexpr (kBeta == 2) beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
-        else if constexpr (kBeta == 1) beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, c, ds);
-        else beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, c, ds);
+        const int lid_y = d.lid_y, wall_y = d.wall_y;
+        if constexpr (kAlpha) alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
+        else if constexpr (kBeta >= 3) beta_cells_pk<St, CPT, kBeta == 4>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
+        else if constexpr (kBeta == 2) beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
+        else if constexpr (kBeta == 1) beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
+        else beta_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
     }
 }
 
@@ -784,7 +1022,9 @@ cudaError_t launch_batch_kernel(const BatchArgs& a, cudaStream_t st)
     constexpr FastVariant fv = kFastMenu[VARIANT];
     constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha, fv.direct ? 2 : fv.block_exchange ? 1 : 0>;
+    constexpr bool pk = fv.packed != 0 && sizeof(typename St::bits) == 2;
+    auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha,
+                           pk ? 2 + fv.packed : fv.direct ? 2 : fv.block_exchange ? 1 : 0>;
     int dev = 0, sms = 0, per_sm = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -31,6 +31,8 @@ struct lbm_solver {
     int lid_y = -1;                 // fast path: lid row (ny) or 0 for none; -1: flag-array path
     int variant = 0;                // launch variant of the vectorised kernels
     bool fma = false;               // FP64: fused multiply-adds in the vectorised steps
+    int lid_mode = 0;               // LBM_LID_INJECTION or LBM_LID_MOVING_WALL; the wall moves
+                                    // while p.wall_y > 0
     cudaStream_t capture_stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     int64_t device_bytes = 0;

@@ -2,13 +2,15 @@
 //
 // Checkpoint file (little-endian):
 //   char[16]  "LBMGB300CKPT" padded with zeros
-//   uint32    version (1)
+//   uint32    version (2; version-1 files, without the lid record, are read
+//             as the injection lid)
 //   int32     storage, nx, ny, nz
 //   int64     step counter
 //   int32     last step was alpha, FP64 fused multiply-adds (0/1)
 //   double    inv_tau, lid velocity, gravity x, y, z
 //   int32     boundary[6]
 //   uint64    flag bytes, population bytes
+//   int32     lid mode, moving wall (0/1)            -- version 2 only
 //   uint8     flags of the (nx+2)(ny+2)(nz+2) cells, x fastest
 //   raw       populations: 19 slots of the same cells in the storage type
 //             (16-bit storage: the stored deviations, bit for bit)
@@ -44,6 +46,10 @@ struct CkptHeader {
     double inv_tau, lid_u, gx, gy, gz;
     int32_t boundary[6];
     uint64_t flag_bytes, pop_bytes;
+};
+// Appended by version 2.
+struct CkptLid {
+    int32_t lid_mode, moving_wall;
 };
 #pragma pack(pop)
 
@@ -106,7 +112,8 @@ int lbm_save_checkpoint(lbm_solver* s, const char* path)
     CkptHeader h;
     std::memset(&h, 0, sizeof(h));
     std::memcpy(h.magic, kMagic, 16);
-    h.version = 1;
+    h.version = 2;
+    const CkptLid lid = {s->lid_mode, s->p.wall_y > 0 ? 1 : 0};
     h.storage = s->storage;
     h.nx = g.nx; h.ny = g.ny; h.nz = g.nz;
     h.counter = s->counter;
@@ -127,7 +134,8 @@ int lbm_save_checkpoint(lbm_solver* s, const char* path)
         File out;
         out.f = std::fopen(tmp.c_str(), "wb");
         if (!out.f) return fail(LBM_ERR_IO, "cannot write checkpoint \"%s\"", tmp.c_str());
-        if (std::fwrite(&h, sizeof(h), 1, out.f) != 1 || std::fwrite(flags.data(), 1, cells, out.f) != cells ||
+        if (std::fwrite(&h, sizeof(h), 1, out.f) != 1 || std::fwrite(&lid, sizeof(lid), 1, out.f) != 1 ||
+            std::fwrite(flags.data(), 1, cells, out.f) != cells ||
             std::fwrite(pops.data(), 1, pops.size(), out.f) != pops.size())
             return fail(LBM_ERR_IO, "short write to \"%s\"", tmp.c_str());
         if (std::fflush(out.f) != 0) return fail(LBM_ERR_IO, "cannot flush \"%s\"", tmp.c_str());
@@ -137,15 +145,25 @@ int lbm_save_checkpoint(lbm_solver* s, const char* path)
 }
 
 // Reads the header and validates it against a solver (or returns it).
-static int read_header(FILE* f, const char* path, CkptHeader& h)
+static int read_header(FILE* f, const char* path, CkptHeader& h, CkptLid& lid)
 {
     if (std::fread(&h, sizeof(h), 1, f) != 1) return fail(LBM_ERR_IO, "\"%s\": truncated header", path);
-    if (std::memcmp(h.magic, kMagic, 16) != 0 || h.version != 1)
-        return fail(LBM_ERR_IO, "\"%s\" is not a version-1 checkpoint of this solver", path);
-    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_F16SR || h.nx <= 0 || h.ny <= 0 || h.nz <= 0 ||
-        (h.fma != 0 && h.fma != 1))
+    if (std::memcmp(h.magic, kMagic, 16) != 0 || (h.version != 1 && h.version != 2))
+        return fail(LBM_ERR_IO, "\"%s\" is not a version-1 or -2 checkpoint of this solver", path);
+    lid = {LBM_LID_INJECTION, 0};
+    if (h.version == 2) {
+        if (std::fread(&lid, sizeof(lid), 1, f) != 1) return fail(LBM_ERR_IO, "\"%s\": truncated header", path);
+        if ((lid.lid_mode != LBM_LID_INJECTION && lid.lid_mode != LBM_LID_MOVING_WALL) ||
+            (lid.moving_wall != 0 && lid.moving_wall != 1) || (lid.moving_wall && !lid.lid_mode))
+            return fail(LBM_ERR_IO, "\"%s\": corrupt header", path);
+    }
+    // each axis within lbm_create's limit [1, 2^20], so the products below
+    // are exact in 64 bits
+    const auto axis_ok = [](int32_t n) { return n > 0 && n <= (1 << 20); };
+    if (h.storage < LBM_STORAGE_F64 || h.storage > LBM_STORAGE_F16SR || !axis_ok(h.nx) || !axis_ok(h.ny) ||
+        !axis_ok(h.nz) || (h.fma != 0 && h.fma != 1))
         return fail(LBM_ERR_IO, "\"%s\": corrupt header", path);
-    const uint64_t cells = (uint64_t)(h.nx + 2) * (h.ny + 2) * (h.nz + 2);
+    const uint64_t cells = ((uint64_t)h.nx + 2) * ((uint64_t)h.ny + 2) * ((uint64_t)h.nz + 2);
     if (h.flag_bytes != cells || h.pop_bytes != (uint64_t)lbm::Q * cells * (uint64_t)elem_bytes(h.storage))
         return fail(LBM_ERR_IO, "\"%s\": sizes do not match the header", path);
     return LBM_OK;
@@ -158,10 +176,14 @@ int lbm_load_checkpoint(lbm_solver* s, const char* path)
     in.f = std::fopen(path, "rb");
     if (!in.f) return fail(LBM_ERR_IO, "cannot read checkpoint \"%s\"", path);
     CkptHeader h;
-    if (int r = read_header(in.f, path, h)) return r;
+    CkptLid lid;
+    if (int r = read_header(in.f, path, h, lid)) return r;
     if (h.storage != s->storage || h.nx != s->g.nx || h.ny != s->g.ny || h.nz != s->g.nz)
         return fail(LBM_ERR_INVALID_ARGUMENT, "\"%s\" holds a %dx%dx%d domain of storage %d", path, h.nx, h.ny, h.nz,
                     h.storage);
+    if (lid.lid_mode != s->lid_mode)
+        return fail(LBM_ERR_INVALID_ARGUMENT, "\"%s\" was written with lid mode %d, the solver has %d", path,
+                    lid.lid_mode, s->lid_mode);
     std::vector<unsigned char> flags((size_t)h.flag_bytes);
     std::vector<unsigned char> pops((size_t)h.pop_bytes);
     if (std::fread(flags.data(), 1, flags.size(), in.f) != flags.size() ||
@@ -176,6 +198,13 @@ int lbm_load_checkpoint(lbm_solver* s, const char* path)
     s->counter = h.counter;
     s->last_alpha = h.last_alpha != 0;
     s->macros_fresh = false;
+    if ((s->p.wall_y > 0) != (lid.moving_wall != 0)) {  // the wall's state as saved; graphs hold the old one
+        s->p.wall_y = lid.moving_wall ? s->g.ny : 0;
+        if (s->graph) {
+            cudaGraphExecDestroy(s->graph);
+            s->graph = nullptr;
+        }
+    }
     return LBM_OK;
 }
 
@@ -184,11 +213,12 @@ int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** ou
     if (!path || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
     CkptHeader h;
+    CkptLid lid;
     {
         File in;
         in.f = std::fopen(path, "rb");
         if (!in.f) return fail(LBM_ERR_IO, "cannot read checkpoint \"%s\"", path);
-        if (int r = read_header(in.f, path, h)) return r;
+        if (int r = read_header(in.f, path, h, lid)) return r;
     }
     lbm_params p;
     std::memset(&p, 0, sizeof(p));
@@ -200,6 +230,7 @@ int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** ou
     p.gravity[0] = h.gx; p.gravity[1] = h.gy; p.gravity[2] = h.gz;
     p.device = device;
     p.fused_multiply_add = h.fma;  // resume with the arithmetic that wrote the checkpoint
+    p.lid_mode = lid.lid_mode;
     lbm_solver* s = nullptr;
     if (int r = lbm_create(&p, &s)) return r;
     if (int r = lbm_load_checkpoint(s, path)) {

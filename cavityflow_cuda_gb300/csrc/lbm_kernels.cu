@@ -33,6 +33,20 @@ __device__ __forceinline__ long long wrapped_position(const Grid& g, int x, int 
     return g.idx(xn, yn, zn);
 }
 
+// The moving top wall on the flag-array path: a FLUID cell of row
+// prm.wall_y takes wall_correct for each of its links 4 (+x+y) and 7 (-x+y)
+// that end in an OBSTACLE cell of the row above (the moving face).
+template <class St>
+__device__ __forceinline__ void wall_correct_flagged(typename St::T* f, const uint8_t* __restrict__ flags,
+                                                     const Grid& g, const Params& prm, int x, int y, int z)
+{
+    using T = typename St::T;
+    if (prm.wall_y <= 0 || y != prm.wall_y || x < 1 || x > g.nx || z < 1 || z > g.nz) return;
+    const T du = wall_shift<St>(T(prm.lid_u));
+    if (flags[g.ref(x + 1, y + 1, z)] == kObstacle) f[5] -= du;
+    if (flags[g.ref(x - 1, y + 1, z)] == kObstacle) f[6] += du;
+}
+
 template <class St, bool kGravity>
 __global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t* __restrict__ flags,
                               const Grid g, const Params prm, const int3 o, const int3 s)
@@ -52,6 +66,7 @@ __global__ void alpha_general(typename St::bits* __restrict__ dd, const uint8_t*
     if (fl == kFluid) {
 #pragma unroll
         for (int k = 0; k < Q; ++k) f[k] = St::load_step(dd[k * g.S + c0]);
+        wall_correct_flagged<St>(f, flags, g, prm, x, y, z);
         if (kGravity) collide_fluid_gravity(f, inv_tau, T(prm.gx), T(prm.gy), T(prm.gz));
         else collide<St>(f, inv_tau);
     } else {
@@ -87,7 +102,10 @@ __global__ void beta_general(typename St::bits* __restrict__ dd, const uint8_t* 
     T f[Q];
 #pragma unroll
     for (int k = 0; k < Q; ++k) f[opp(k)] = St::load_step(dd[pos[k]]);
-    if (fl == kFluid) collide<St>(f, T(prm.inv_tau));
+    if (fl == kFluid) {
+        wall_correct_flagged<St>(f, flags, g, prm, x, y, z);
+        collide<St>(f, T(prm.inv_tau));
+    }
     else if (fl == kInjection) inject_step<St>(f, St::shifted ? T(0) : T(1), T(prm.lid_u));
     // GHOST_LAYER (and any other value): streamed through unchanged (a value
     // read from storage is stored back exactly, also by stochastic rounding)
@@ -441,7 +459,7 @@ bool fast_variant_fits(int storage, int variant, const Grid& g)
     if (variant < 0 || variant >= kFastVariantCount) return false;
     if (variant < kRegisterVariants) return true;
     const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
-    const int elem = storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 ? 4 : 2;
+    const int elem = storage_elem_bytes(storage);
     if (!default_layout(g, elem)) return false;  // the bulk-copy kernels run on the default layout only
     int dev = 0, max_optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
@@ -460,7 +478,7 @@ void fast_variant_shape(int storage, int variant, bool alpha, int nx, int& cpt, 
         return;
     }
     const KernelShape k = alpha ? kFastMenu[variant].alpha : kFastMenu[variant].beta;
-    const int V = 16 / (storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 ? 4 : 2);
+    const int V = 16 / storage_elem_bytes(storage);
     cpt = V / k.cpt_div > 0 ? V / k.cpt_div : 1;
     block = k.block;
 }
@@ -518,7 +536,10 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
         case kStorageF64Fma:
             e = launch_tma_f64(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st);
             break;
-        case 1: e = launch_tma_f32(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
+        case 1:
+        case kStorageF32Fma:
+            e = launch_tma_f32(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st);
+            break;
         case 2: e = launch_tma_f16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 3: e = launch_tma_bf16s(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
         case 4: e = launch_tma_f16sr(alpha, dd, g, p, lid_y, c.rows, c.stages, c.consumer_warps, err, st); break;
@@ -532,6 +553,7 @@ cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, con
     case 0: return launch_fast_f64(variant, alpha, dd, g, p, lid_y, st);
     case kStorageF64Fma: return launch_fast_f64fma(variant, alpha, dd, g, p, lid_y, st);
     case 1: return launch_fast_f32(variant, alpha, dd, g, p, lid_y, st);
+    case kStorageF32Fma: return launch_fast_f32fma(variant, alpha, dd, g, p, lid_y, st);
     case 2: return launch_fast_f16s(variant, alpha, dd, g, p, lid_y, st);
     case 3: return launch_fast_bf16s(variant, alpha, dd, g, p, lid_y, st);
     case 4: return launch_fast_f16sr(variant, alpha, dd, g, p, lid_y, st);

@@ -60,13 +60,18 @@ struct KernelShape {
 // one-cell-shifted windows of the c_x = +-1 slots itself with element-aligned
 // accesses (2-4 per window), so there are no shuffles, shared memory or
 // barriers and no row- or block-edge cases.
+// `packed` (16-bit storage; other storages run the direct beta): the direct
+// windows with two cells per 32-bit word and paired conversions
+// (beta_fast_pk), loading each window as its pieces (1) or as the aligned
+// vector plus one element (2).
 struct FastVariant {
     KernelShape alpha;
     KernelShape beta;
     bool block_exchange;
     bool direct = false;
+    int packed = 0;
 };
-constexpr int kRegisterVariants = 18;
+constexpr int kRegisterVariants = 22;
 constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
     {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
@@ -86,6 +91,10 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 64, 4}, {2, 64, 8}, false, true},    // alpha 16-byte, beta 8-byte, direct
     {{1, 64, 4}, {1, 64, 4}, false, true},    // 16-byte vectors, two-warp blocks, direct
     {{2, 256, 2}, {2, 256, 2}, false, true},  // 8-byte vectors, eight-warp blocks, direct
+    {{1, 64, 4}, {2, 64, 10}, false, true, 1},  // alpha 16-byte; beta 8-byte packed pieces, <= 102 registers
+    {{1, 64, 4}, {2, 64, 8}, false, true, 1},   // the same, <= 128 registers
+    {{1, 64, 4}, {2, 64, 10}, false, true, 2},  // alpha 16-byte; beta 8-byte packed, vector loads
+    {{1, 64, 4}, {2, 64, 8}, false, true, 2},   // the same, <= 128 registers
 };
 struct TmaConfig {
     int rows;            // rows per work unit
@@ -98,9 +107,16 @@ constexpr TmaConfig kTmaMenu[kTmaVariants] = {
 };
 constexpr int kFastVariantCount = kRegisterVariants + kTmaVariants;
 // Storage code of the FP64 step kernels with fused multiply-adds (F64F, built
-// in fast_f64_fma.cu); accepted by launch_fast_step, fast_variant_fits and
+// in fast_fma.cu); accepted by launch_fast_step, fast_variant_fits and
 // fast_variant_shape only.  Its bulk-copy variants run the unfused kernels.
 constexpr int kStorageF64Fma = 5;
+// The same for FP32 (F32F); its bulk-copy variants run the unfused kernels.
+constexpr int kStorageF32Fma = 6;
+// Bytes per stored population of a storage code (kernel storage codes included).
+inline int storage_elem_bytes(int storage)
+{
+    return storage == 0 || storage == kStorageF64Fma ? 8 : storage == 1 || storage == kStorageF32Fma ? 4 : 2;
+}
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
                              int lid_y, int* err, cudaStream_t st);
 // Whether a variant fits this domain (shared memory of the bulk-copy kernels).
@@ -131,6 +147,8 @@ cudaError_t launch_batch_map(const BatchDomain* doms, int ndom, long long vblock
 cudaError_t launch_fast_f64(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);
 cudaError_t launch_fast_f64fma(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
+                               cudaStream_t st);
+cudaError_t launch_fast_f32fma(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                                cudaStream_t st);
 cudaError_t launch_fast_f32(int variant, bool alpha, void* dd, const Grid& g, const Params& p, int lid_y,
                             cudaStream_t st);

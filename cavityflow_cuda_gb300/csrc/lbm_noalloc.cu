@@ -40,9 +40,9 @@ __global__ void __launch_bounds__(kNoAllocBlock) noalloc_plane_sums(const T* __r
     const long long X = nx + 2, XY = X * (ny + 2), C = XY * (nz + 2);
     const int z = blockIdx.x + 1;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    const int cells = nx * ny;
-    for (int i = threadIdx.x; i < cells; i += kNoAllocBlock) {
-        const int x = 1 + i % nx, y = 1 + i / nx;
+    const long long cells = (long long)nx * ny;  // 64-bit: i + kNoAllocBlock never wraps
+    for (long long i = threadIdx.x; i < cells; i += kNoAllocBlock) {
+        const long long x = 1 + i % nx, y = 1 + i / nx;
         const long long gid = z * XY + y * X + x;
         const int32_t fl = flags[gid];
         if (fl != kFluid && fl != kInjection) continue;
@@ -88,25 +88,74 @@ __global__ void noalloc_total(const double* __restrict__ partials, int nz, doubl
 
 namespace {
 
-// Device address of g_noalloc_partials on the current device, looked up once
-// per device.  In host code the array's name is only a host-side stand-in, so
-// the kernels receive this address instead.
+// The driver calls that name the current context, resolved through the
+// runtime (the library links no driver library).
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+
+// Device address of g_noalloc_partials in the CURRENT context.  In host code
+// the array's name is only a host-side stand-in, so the kernels receive this
+// address instead.  The array is instantiated once per context (a
+// cudaDeviceReset, or a caller's own driver context, gives a new one at a
+// new address), so the address is cached by the context's unique id: the
+// first call in each context -- for the usual caller, the first call on each
+// device, in its primary context -- does the lookup.
 int scratch_address(double** out)
 {
     static std::mutex mu;
-    static double* addr[256] = {nullptr};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
-        return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: no current device");
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    struct Entry {
+        unsigned long long ctx_id;
+        double* addr;
+    };
+    static Entry cache[64];
+    static int used = 0;
+    static int next = 0;
+
+    cudaError_t e = cudaSuccess;
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, lbm::g_noalloc_partials);
-        if (e != cudaSuccess) return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: cudaGetSymbolAddress: %s",
-                                                      cudaGetErrorString(e));
-        addr[dev] = static_cast<double*>(p);
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: driver context queries unavailable");
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
     }
-    *out = addr[dev];
+    void* ctx = nullptr;
+    void* p = nullptr;
+    if (get_current(&ctx) != 0) return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: cuCtxGetCurrent failed");
+    if (!ctx) {
+        // No context current on this thread yet: the runtime's symbol lookup
+        // initialises the current device's primary context and makes it current.
+        e = cudaGetSymbolAddress(&p, lbm::g_noalloc_partials);
+        if (e != cudaSuccess)
+            return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: cudaGetSymbolAddress: %s",
+                                     cudaGetErrorString(e));
+        if (get_current(&ctx) != 0 || !ctx)
+            return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: no current CUDA context");
+    }
+    unsigned long long id = 0;
+    if (get_id(ctx, &id) != 0) return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: cuCtxGetId failed");
+    for (int i = 0; i < used; ++i)
+        if (cache[i].ctx_id == id) {
+            *out = cache[i].addr;
+            return LBM_OK;
+        }
+    if (!p) {
+        e = cudaGetSymbolAddress(&p, lbm::g_noalloc_partials);
+        if (e != cudaSuccess)
+            return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc: cudaGetSymbolAddress: %s",
+                                     cudaGetErrorString(e));
+    }
+    // context ids are never reused, so an evicted entry is only looked up again
+    const int slot = used < 64 ? used++ : (next++ & 63);
+    cache[slot] = {id, static_cast<double*>(p)};
+    *out = static_cast<double*>(p);
     return LBM_OK;
 }
 
@@ -138,9 +187,9 @@ extern "C" int lbm_reduce_noalloc(const void* populations, const int32_t* flags,
         lbm::noalloc_plane_sums<float><<<nz, lbm::kNoAllocBlock, 0, st>>>(static_cast<const float*>(populations),
                                                                          flags, nx, ny, nz, la, partials);
     lbm::noalloc_total<<<1, 32, 0, st>>>(partials, nz, out_device);
-    lbm::add_launches(2);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess)
         return lbm::record_error(LBM_ERR_CUDA, "lbm_reduce_noalloc launch: %s", cudaGetErrorString(e));
+    lbm::add_launches(2);
     return LBM_OK;
 }

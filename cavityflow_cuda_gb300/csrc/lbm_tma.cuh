@@ -144,6 +144,7 @@ template <class St, bool kAlpha>
 __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __restrict__ dd, const Grid g,
                                                            const typename St::T inv_tau,
                                                            const typename St::T lid_u, const int lid_y,
+                                                           const int wall_y,
                                                            const int R, const int stages, int* __restrict__ err,
                                                            const uint32_t* __restrict__ step_base,
                                                            const uint32_t step_off)
@@ -240,6 +241,7 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
     const int nconsumer = nwarps_c * 32;
     const int lane = threadIdx.x & 31;
     const T rho0 = St::shifted ? T(0) : T(1);
+    const T du = wall_shift<St>(lid_u);
     for (long long i = 0; i < mine; ++i) {
         const int s = (int)(i % stages);
         const uint32_t parity = (uint32_t)(i / stages) & 1u;
@@ -258,12 +260,14 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
         bits* sb = buf + (size_t)s * stage_elems;
         for (int r = 0; r < rn; ++r) {
             const bool lid = (y0 + r == lid_y);
+            const bool wall = (y0 + r == wall_y);
             for (int x = 1 + ctid; x <= g.nx; x += nconsumer) {
                 const unsigned col = (unsigned)(r * g.P + x + g.xoff);
                 T f[Q];
                 if constexpr (kAlpha) {
 #pragma unroll
                     for (int k = 0; k < Q; ++k) f[k] = St::load_step(sb[k * slot_elems + col]);
+                    if (wall) wall_correct(f, du);
                     if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
                     uint32_t h = 0;
@@ -273,6 +277,7 @@ __global__ void __launch_bounds__(kTmaMaxThreads) step_tma(typename St::bits* __
                 } else {
 #pragma unroll
                     for (int k = 0; k < Q; ++k) f[opp(k)] = St::load_step(sb[k * slot_elems + col + dir_x(k)]);
+                    if (wall) wall_correct(f, du);
                     if (lid) inject_step<St>(f, rho0, lid_u);
                     else collide<St>(f, inv_tau);
                     uint32_t h = 0;
@@ -325,7 +330,7 @@ cudaError_t launch_tma_impl(bool alpha, void* dd, const Grid& g, const Params& p
     if (per_sm < 1) return cudaErrorInvalidValue;
     const long long units = (long long)((g.ny + R - 1) / R) * g.nz;
     const long long grid = units < (long long)per_sm * sms ? units : (long long)per_sm * sms;
-    kern<<<(int)grid, threads, smem, st>>>(static_cast<bits*>(dd), g, T(p.inv_tau), T(p.lid_u), lid_y, R, stages,
+    kern<<<(int)grid, threads, smem, st>>>(static_cast<bits*>(dd), g, T(p.inv_tau), T(p.lid_u), lid_y, p.wall_y, R, stages,
                                           err, p.step_base, p.step_off);
     return cudaGetLastError();
 }

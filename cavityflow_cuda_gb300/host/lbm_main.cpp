@@ -3,8 +3,8 @@
 // src/CManager.cpp:27-105 for one subdomain, CController::run
 // src/CController.cpp:1354-1510) on the C ABI of liblbm_gb300.so.
 //
-//   lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--device N]
-//             [--fast-variant V | --autotune] [--vtk-binary]
+//   lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--fma] [--moving-wall]
+//             [--device N] [--fast-variant V | --autotune] [--vtk-binary]
 //             [--checkpoint FILE --checkpoint-every N] [--resume FILE]
 //
 // As the reference: the six faces are obstacles, the lid (y = ny) is driven
@@ -60,6 +60,7 @@ struct Options {
     int device = 0;
     int fast_variant = -1;
     bool fma = false;
+    int lid_mode = LBM_LID_INJECTION;
     bool autotune = false;
     bool vtk_binary = false;
     std::string checkpoint;
@@ -69,7 +70,8 @@ struct Options {
 
 void usage()
 {
-    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--fma] [--device N]\n"
+    std::cerr << "usage: lbm_gb300 CONFIG.xml [--storage f64|f32|f16s|bf16s|f16sr] [--fma] [--moving-wall]\n"
+                 "                 [--device N]\n"
                  "                 [--fast-variant V | --autotune] [--vtk-binary]\n"
                  "                 [--checkpoint FILE --checkpoint-every N] [--resume FILE]\n";
 }
@@ -99,7 +101,9 @@ Options parse(int argc, char** argv)
         } else if (a == "--fast-variant") {
             o.fast_variant = std::atoi(value().c_str());
         } else if (a == "--fma") {
-            o.fma = true;  // FP64: fused multiply-adds (lbm_params.fused_multiply_add)
+            o.fma = true;  // FP64/FP32: fused multiply-adds (lbm_params.fused_multiply_add)
+        } else if (a == "--moving-wall") {
+            o.lid_mode = LBM_LID_MOVING_WALL;  // mass-conserving moving top wall instead of the injection lid
         } else if (a == "--autotune") {
             o.autotune = true;
         } else if (a == "--vtk-binary") {
@@ -200,6 +204,7 @@ int main(int argc, char** argv)
         p.device = opt.device;
         p.fast_variant = opt.fast_variant < 0 ? 0 : opt.fast_variant + 1;
         p.fused_multiply_add = opt.fma ? 1 : 0;
+        p.lid_mode = opt.lid_mode;
         check(lbm_create(&p, &solver), "lbm_create");
         check(lbm_set_driven_cavity(solver), "lbm_set_driven_cavity");
     }

@@ -25,6 +25,8 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "lbm_gb300.h")
 OBSTACLE, FLUID, VELOCITY_INJECTION, GHOST_LAYER = 1, 2, 4, 8
 DIRECTION_ALL, LEFT, RIGHT, BOTTOM, TOP, BACK, FRONT = -1, 0, 1, 2, 3, 4, 5
 STORAGE = {"f64": 0, "f32": 1, "f16s": 2, "bf16s": 3, "f16sr": 4}
+# lbm_params.lid_mode: the reference's injection lid, or the moving top wall
+LID_MODES = {"injection": 0, "wall": 1}
 
 _lib: Optional[C.CDLL] = None
 
@@ -64,7 +66,7 @@ class _Params(C.Structure):
     _fields_ = [("size", C.c_int32 * 3), ("storage", C.c_int32), ("boundary", C.c_int32 * 6),
                 ("inv_tau", C.c_double), ("lid_velocity", C.c_double), ("gravity", C.c_double * 3),
                 ("device", C.c_int32), ("fast_variant", C.c_int32), ("fused_multiply_add", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("lid_mode", C.c_int32)]
 
 
 class _Info(C.Structure):
@@ -74,7 +76,8 @@ class _Info(C.Structure):
                 ("block_threads", C.c_int32), ("beta_cells_per_thread", C.c_int32),
                 ("beta_block_threads", C.c_int32), ("beta_block_exchange", C.c_int32),
                 ("fused_multiply_add", C.c_int32), ("row_pitch", C.c_int64), ("slot_stride", C.c_int64),
-                ("device_bytes", C.c_int64), ("x1_column", C.c_int64)]
+                ("device_bytes", C.c_int64), ("x1_column", C.c_int64), ("lid_mode", C.c_int32),
+                ("moving_wall", C.c_int32)]
 
 
 def declared_functions() -> list[str]:
@@ -244,7 +247,7 @@ class CLbmSolverGB300:
     def __init__(self, size: Sequence[int], inv_tau: float, lid_velocity: float, storage: str = "f32",
                  boundary: Sequence[int] = (OBSTACLE,) * 6, gravity: Sequence[float] = (0.0, 0.0, 0.0),
                  device: int = 0, driven_cavity: bool = True, fast_variant: int = -1,
-                 fused_multiply_add: bool = False):
+                 fused_multiply_add: bool = False, lid: str = "injection"):
         self._lib = load_library()
         p = _Params()
         p.size[:] = [int(s) for s in size]
@@ -256,6 +259,7 @@ class CLbmSolverGB300:
         p.device = int(device)
         p.fast_variant = 0 if fast_variant < 0 else int(fast_variant) + 1
         p.fused_multiply_add = 1 if fused_multiply_add else 0
+        p.lid_mode = LID_MODES[lid]
         h = C.c_void_p()
         _check(self._lib.lbm_create(C.byref(p), C.byref(h)))
         self._h = h

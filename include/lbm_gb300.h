@@ -38,7 +38,7 @@
 extern "C" {
 #endif
 
-#define LBM_GB300_ABI_VERSION 1
+#define LBM_GB300_ABI_VERSION 2
 
 /* ---- status codes -------------------------------------------------------- */
 typedef enum lbm_status {
@@ -80,6 +80,24 @@ typedef enum lbm_storage {
     LBM_STORAGE_BF16S = 3,
     LBM_STORAGE_F16SR = 4
 } lbm_storage;
+
+/* How the lid drives the cavity (lbm_params.lid_mode).
+ *
+ * LBM_LID_INJECTION (default) is the reference's lid: lbm_set_driven_cavity
+ * marks the interior plane y = ny as VELOCITY_INJECTION, and every step
+ * resets those cells to feq(rho = 1, u = (U, 0, 0))
+ * (src/CController.cpp:1289-1348, src/gpukernels/lbm_alpha.cu:376-511,
+ * src/gpukernels/lbm_beta.cu:661-732).  The reset adds or removes mass, so
+ * the total mass drifts.
+ *
+ * LBM_LID_MOVING_WALL has no counterpart in the reference: the top face
+ * y = ny + 1 is a wall moving at U along x, and the interior plane y = ny
+ * stays FLUID.  Populations the wall sends back to the fluid carry Ladd's
+ * moving-wall correction -6 w_i (c_i . U) (rho_w = 1).  Both corrections of a
+ * cell cancel, so the total mass of lbm_reduce is conserved to rounding
+ * (FP64: 1e-10 relative and far below).  lbm_set_driven_cavity starts the wall
+ * moving and touches no flags.  The top face must be OBSTACLE. */
+enum { LBM_LID_INJECTION = 0, LBM_LID_MOVING_WALL = 1 };
 
 /* ---- parameters ----------------------------------------------------------- */
 
@@ -171,18 +189,21 @@ typedef struct lbm_params {
                                    variant v of the vectorised kernels,
                                    v < lbm_fast_variant_count(); see
                                    lbm_autotune                                */
-    int32_t fused_multiply_add; /* FP64 storage only.  0 (default): the
+    int32_t fused_multiply_add; /* F64 and F32 storage.  0 (default): the
                                    collision performs the reference CPU
                                    kernels' unfused IEEE operations (results
                                    bit-identical to them).  1: the vectorised
                                    register-variant steps fuse its
-                                   multiply-adds, as the reference's nvcc build
-                                   does: faster on GB300's FP64 units, within
-                                   1e-15 of the reference CUDA kernels after
-                                   1000 steps, no longer bit-identical to the
-                                   CPU kernels.  Flag-array and bulk-copy steps
-                                   stay unfused.                               */
-    int32_t reserved;           /* zero                                        */
+                                   multiply-adds (and FP32 flushes subnormals),
+                                   as the reference's nvcc build
+                                   (-use_fast_math) does: the closest match to
+                                   the reference CUDA kernels, and faster on
+                                   GB300's FP64 units; no longer
+                                   bit-identical to the CPU kernels.
+                                   Flag-array and bulk-copy steps stay
+                                   unfused.                                    */
+    int32_t lid_mode;           /* LBM_LID_INJECTION (0, the reference's lid)
+                                   or LBM_LID_MOVING_WALL                      */
 } lbm_params;
 
 typedef struct lbm_solver lbm_solver;   /* opaque */
@@ -205,7 +226,9 @@ typedef struct lbm_info {
     int32_t beta_block_exchange;    /* how beta gets the one-cell-shifted
                                        slots: 0 warp shuffles (beta_fast), 1
                                        across the block (beta_fast_blk), 2 no
-                                       exchange (beta_fast_direct)             */
+                                       exchange (beta_fast_direct), 3 no
+                                       exchange with two 16-bit cells per
+                                       register (beta_fast_pk)                 */
     int32_t fused_multiply_add;     /* lbm_params.fused_multiply_add           */
     int64_t row_pitch;          /* elements per padded x row on the device     */
     int64_t slot_stride;        /* elements per population slot                */
@@ -213,6 +236,9 @@ typedef struct lbm_info {
     int64_t x1_column;          /* column of interior cell x = 1 in a row: 32
                                    bytes in (the default), or 16 for the
                                    packed rows of batch domains               */
+    int32_t lid_mode;           /* lbm_params.lid_mode                         */
+    int32_t moving_wall;        /* 1 while the top wall moves (moving-wall
+                                   mode after lbm_set_driven_cavity)           */
 } lbm_info;
 
 /* ---- lifecycle ------------------------------------------------------------ */
@@ -239,7 +265,8 @@ int lbm_value_size(const lbm_solver* solver);
 
 /* Marks the lid plane y = ny (x in [1,nx], z in [1,nz]) as
  * VELOCITY_INJECTION.  Replaces CController<T>::setDrivenCavitySzenario
- * (src/CController.cpp:1289-1348). */
+ * (src/CController.cpp:1289-1348).  In LBM_LID_MOVING_WALL mode it sets the
+ * top wall moving instead and changes no flag. */
 int lbm_set_driven_cavity(lbm_solver* solver);
 
 /* ---- time steps -------------------------------------------------------------
@@ -281,11 +308,12 @@ int lbm_selftest_bounded_wait(lbm_solver* solver, int32_t limit_us);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: 18 register-blocked
- * vector kernels (0..17: cells per thread, threads per block and blocks per
+/* Number of launch variants of the box-cavity kernels: 22 register-blocked
+ * vector kernels (0..21: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
- * elements per warp, per block or not at all) and 6 row-pipelined bulk-copy
- * kernels (18..23: rows per unit, buffers, consumer warps). */
+ * elements per warp, per block or not at all; 18..21 keep 16-bit populations
+ * two cells per register) and 6 row-pipelined bulk-copy kernels (22..27: rows
+ * per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Number of register variants (the first variants; the batch kernel's menu). */
 int lbm_register_variant_count(void);
@@ -361,9 +389,12 @@ int lbm_reduce(lbm_solver* solver, double out[4], void* stream);
  * nz > 4096 are rejected with LBM_ERR_INVALID_ARGUMENT.  All calls share that
  * array, so calls that overlap on the GPU (different streams, or different
  * host threads on one device) race and must be serialised by the caller.
- * The first call on each device looks up the array's device address with
- * cudaGetSymbolAddress (with that device current); make that first call
- * before any stream capture. */
+ * The array has its own device address in each CUDA context.  The first call
+ * in a context (for most callers: the first call on each device, in its
+ * primary context) looks that address up with cudaGetSymbolAddress, with the
+ * device current, and caches it by the context's unique id, so a
+ * cudaDeviceReset or a caller's own driver context gets a fresh lookup; make
+ * that first call before any stream capture. */
 int lbm_reduce_noalloc(const void* populations, const int32_t* flags, const int32_t size[3], int32_t storage,
                        int32_t last_step_was_alpha, double* out_device, void* stream);
 

@@ -244,11 +244,25 @@ void orc_init_s(uint16_t* dd, int32_t* flags, int nx, int ny, int nz, const int3
     memset(dd, 0, (size_t)C * 19 * sizeof(uint16_t));
 }
 
-void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                 int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+/* The moving top wall's correction in step units (see wall_correctf). */
+static float wall_du(float lid_u, int kind)
+{
+    float du = lid_u * (1.0f / 6.0f);
+    if (kind == 2) du *= kSrScale;
+    return du;
+}
+static int wall_row(int wall, const int32_t origin[3], int Xi, int Yi, int Zi, int nx, int ny, int nz)
+{
+    return wall && origin[1] + Yi == ny && origin[0] + Xi >= 1 && origin[0] + Xi <= nx && origin[2] + Zi >= 1 &&
+           origin[2] + Zi <= nz;
+}
+
+static void alpha_s_impl(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                         int kind, const int32_t origin[3], const int32_t size[3], uint32_t step, int wall)
 {
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
+    const float du = wall_du(lid_u, kind);
     int Zi;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
@@ -265,6 +279,7 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
                 fl = flags[gid];
                 if (fl == ORC_FLUID) {
                     for (k = 0; k < 19; ++k) f[k] = ld16_step(dd[k * C + gid], kind);
+                    if (wall_row(wall, origin, Xi, Yi, Zi, nx, ny, nz)) wall_correctf(f, flags, gid, X, du);
                     collide_shifted(f, inv_tau, step_log2(kind));
                 } else if (fl == ORC_VELOCITY_INJECTION) {
                     lid_step(lid_u, kind, f);
@@ -279,11 +294,24 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
     }
 }
 
-void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
-                int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                 int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+{
+    alpha_s_impl(dd, flags, nx, ny, nz, inv_tau, lid_u, kind, origin, size, step, 0);
+}
+
+void orc_alpha_wall_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                      int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+{
+    alpha_s_impl(dd, flags, nx, ny, nz, inv_tau, lid_u, kind, origin, size, step, 1);
+}
+
+static void beta_s_impl(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                        int kind, const int32_t origin[3], const int32_t size[3], uint32_t step, int wall)
 {
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
+    const float du = wall_du(lid_u, kind);
     int64_t delta[19];
     int Zi, k0;
     for (k0 = 0; k0 < 19; ++k0) delta[k0] = beta_deltaf(k0, X, XY, C);
@@ -306,6 +334,7 @@ void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, floa
                 if (fl == ORC_FLUID) {
                     for (k = 0; k < 18; ++k) f[k ^ 1] = ld16_step(dd[pos[k]], kind);
                     f[18] = ld16_step(dd[pos[18]], kind);
+                    if (wall_row(wall, origin, Xi, Yi, Zi, nx, ny, nz)) wall_correctf(f, flags, gid, X, du);
                     collide_shifted(f, inv_tau, step_log2(kind));
                     h = sr_cell(sr_hash((uint32_t)(gid - (origin[0] + Xi)), step), origin[0] + Xi);
                     for (k = 0; k < 19; ++k) dd[pos[k]] = st16k(f[k], kind, h, k);
@@ -322,6 +351,18 @@ void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, floa
             }
         }
     }
+}
+
+void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+{
+    beta_s_impl(dd, flags, nx, ny, nz, inv_tau, lid_u, kind, origin, size, step, 0);
+}
+
+void orc_beta_wall_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                     int kind, const int32_t origin[3], const int32_t size[3], uint32_t step)
+{
+    beta_s_impl(dd, flags, nx, ny, nz, inv_tau, lid_u, kind, origin, size, step, 1);
 }
 
 void orc_macros_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, int last_was_alpha,

@@ -41,6 +41,17 @@ void orc_macros_d(const double* dd, const int32_t* flags, int nx, int ny, int nz
 void orc_reduce_d(const double* dd, const int32_t* flags, int nx, int ny, int nz,
                   int last_was_alpha, double out[4]);
 
+/* The same steps with the GB300 solver's opt-in moving top wall instead of an
+ * injection lid (no reference counterpart): FLUID cells of row y = ny take
+ * Ladd's correction -6 w_i (c_i . U) on the populations 5 and 6 the top face
+ * sends back (see wall_correct in lbm_oracle_body.h). */
+void orc_alpha_wall_d(double* dd, const int32_t* flags, int nx, int ny, int nz,
+                      double inv_tau, double gx, double gy, double gz, double lid_u,
+                      const int32_t origin[3], const int32_t size[3]);
+void orc_beta_wall_d(double* dd, const int32_t* flags, int nx, int ny, int nz,
+                     double inv_tau, double lid_u,
+                     const int32_t origin[3], const int32_t size[3]);
+
 /* ---- float ---- */
 void orc_init_f(float* dd, int32_t* flags, int nx, int ny, int nz, const int32_t bc[6]);
 void orc_alpha_f(float* dd, const int32_t* flags, int nx, int ny, int nz,
@@ -49,6 +60,12 @@ void orc_alpha_f(float* dd, const int32_t* flags, int nx, int ny, int nz,
 void orc_beta_f(float* dd, const int32_t* flags, int nx, int ny, int nz,
                 float inv_tau, float lid_u,
                 const int32_t origin[3], const int32_t size[3]);
+void orc_alpha_wall_f(float* dd, const int32_t* flags, int nx, int ny, int nz,
+                      float inv_tau, float gx, float gy, float gz, float lid_u,
+                      const int32_t origin[3], const int32_t size[3]);
+void orc_beta_wall_f(float* dd, const int32_t* flags, int nx, int ny, int nz,
+                     float inv_tau, float lid_u,
+                     const int32_t origin[3], const int32_t size[3]);
 void orc_macros_f(const float* dd, const int32_t* flags, int nx, int ny, int nz,
                   int last_was_alpha, float lid_u, float* rho, float* jx, float* jy, float* jz);
 void orc_reduce_f(const float* dd, const int32_t* flags, int nx, int ny, int nz,
@@ -62,6 +79,10 @@ void orc_alpha_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, flo
                  int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
 void orc_beta_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
                 int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
+void orc_alpha_wall_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                      int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
+void orc_beta_wall_s(uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, float inv_tau, float lid_u,
+                     int kind, const int32_t origin[3], const int32_t size[3], uint32_t step);
 void orc_macros_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, int last_was_alpha,
                   float lid_u, int kind, float* rho, float* jx, float* jy, float* jz);
 void orc_reduce_s(const uint16_t* dd, const int32_t* flags, int nx, int ny, int nz, int last_was_alpha, int kind,

@@ -146,15 +146,28 @@ void SFX(orc_init_)(REAL* dd, int32_t* flags, int nx, int ny, int nz, const int3
     }
 }
 
-void SFX(orc_alpha_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
-                     REAL inv_tau, REAL gx, REAL gy, REAL gz, REAL lid_u,
-                     const int32_t origin[3], const int32_t size[3])
+/* The GB300 solver's opt-in moving top wall (no reference counterpart): a
+ * FLUID cell of row y = ny reads populations 5 (-x-y) and 6 (+x-y) that the
+ * obstacle cells above it (the top face, moving at U along x) sent back as
+ * bounced populations 4 (+x+y) and 7 (-x+y).  Ladd's moving-wall rule
+ * f_opp(i) = f_i - 6 w_i (c_i . U) (rho_w = 1) adds -U/6 to 5 and +U/6 to 6,
+ * each only where that link ends in an OBSTACLE cell. */
+static void SFX(wall_correct)(REAL* f, const int32_t* flags, int64_t gid, int64_t X, REAL du)
+{
+    if (flags[gid + 1 + X] == ORC_OBSTACLE) f[5] -= du;
+    if (flags[gid - 1 + X] == ORC_OBSTACLE) f[6] += du;
+}
+
+static void SFX(alpha_impl)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                            REAL inv_tau, REAL gx, REAL gy, REAL gz, REAL lid_u,
+                            const int32_t origin[3], const int32_t size[3], int wall)
 {
     /* src/gpukernels/lbm_alpha.cu:22-532: read the 19 slots of a cell, collide,
      * write population k into slot opp(k) of the same cell. */
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
     const int gravity = (gx != (REAL)0) || (gy != (REAL)0) || (gz != (REAL)0);
+    const REAL du = lid_u * ((REAL)1 / (REAL)6);
     int Zi;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
@@ -171,6 +184,9 @@ void SFX(orc_alpha_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
                 if (fl != ORC_FLUID && fl != ORC_VELOCITY_INJECTION) continue;
                 if (fl == ORC_FLUID) {
                     for (k = 0; k < 19; ++k) f[k] = dd[k * C + gid];
+                    if (wall && origin[1] + Yi == ny && origin[0] + Xi >= 1 && origin[0] + Xi <= nx &&
+                        origin[2] + Zi >= 1 && origin[2] + Zi <= nz)
+                        SFX(wall_correct)(f, flags, gid, X, du);
                     SFX(collide_fluid)(f, inv_tau, gravity, gx, gy, gz);
                 } else {
                     SFX(inject)(f, lid_u, gravity, gx, gy, gz);
@@ -180,6 +196,20 @@ void SFX(orc_alpha_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
             }
         }
     }
+}
+
+void SFX(orc_alpha_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                     REAL inv_tau, REAL gx, REAL gy, REAL gz, REAL lid_u,
+                     const int32_t origin[3], const int32_t size[3])
+{
+    SFX(alpha_impl)(dd, flags, nx, ny, nz, inv_tau, gx, gy, gz, lid_u, origin, size, 0);
+}
+
+void SFX(orc_alpha_wall_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                          REAL inv_tau, REAL gx, REAL gy, REAL gz, REAL lid_u,
+                          const int32_t origin[3], const int32_t size[3])
+{
+    SFX(alpha_impl)(dd, flags, nx, ny, nz, inv_tau, gx, gy, gz, lid_u, origin, size, 1);
 }
 
 /* Linear-index neighbour offset of direction k, as the beta kernel forms it
@@ -197,9 +227,9 @@ static int64_t SFX(beta_delta)(int k, int64_t X, int64_t XY, int64_t C)
     return d;
 }
 
-void SFX(orc_beta_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
-                    REAL inv_tau, REAL lid_u,
-                    const int32_t origin[3], const int32_t size[3])
+static void SFX(beta_impl)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                           REAL inv_tau, REAL lid_u,
+                           const int32_t origin[3], const int32_t size[3], int wall)
 {
     /* src/gpukernels/lbm_beta.cu:32-915 (USE_SHARED_MEMORY 0, GRAVITATION 0):
      * population opp(k) arrives from slot k at gid+delta_k; after the
@@ -207,6 +237,7 @@ void SFX(orc_beta_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
      * each pair before the write, which restores what it read. */
     const int64_t X = nx + 2, XY = (int64_t)(nx + 2) * (ny + 2);
     const int64_t C = XY * (nz + 2);
+    const REAL du = lid_u * ((REAL)1 / (REAL)6);
     int64_t delta[19];
     int Zi, k0;
     for (k0 = 0; k0 < 19; ++k0) delta[k0] = SFX(beta_delta)(k0, X, XY, C);
@@ -228,6 +259,9 @@ void SFX(orc_beta_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
                 for (k = 0; k < 18; ++k) f[k ^ 1] = dd[pos[k]];
                 f[18] = dd[pos[18]];
                 if (fl == ORC_FLUID) {
+                    if (wall && origin[1] + Yi == ny && origin[0] + Xi >= 1 && origin[0] + Xi <= nx &&
+                        origin[2] + Zi >= 1 && origin[2] + Zi <= nz)
+                        SFX(wall_correct)(f, flags, gid, X, du);
                     SFX(collide_fluid)(f, inv_tau, 0, 0, 0, 0);
                 } else if (fl == ORC_OBSTACLE) {
                     for (k = 0; k < 18; k += 2) { t = f[k]; f[k] = f[k + 1]; f[k + 1] = t; }
@@ -238,6 +272,20 @@ void SFX(orc_beta_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
             }
         }
     }
+}
+
+void SFX(orc_beta_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                    REAL inv_tau, REAL lid_u,
+                    const int32_t origin[3], const int32_t size[3])
+{
+    SFX(beta_impl)(dd, flags, nx, ny, nz, inv_tau, lid_u, origin, size, 0);
+}
+
+void SFX(orc_beta_wall_)(REAL* dd, const int32_t* flags, int nx, int ny, int nz,
+                         REAL inv_tau, REAL lid_u,
+                         const int32_t origin[3], const int32_t size[3])
+{
+    SFX(beta_impl)(dd, flags, nx, ny, nz, inv_tau, lid_u, origin, size, 1);
 }
 
 /* Post-collision populations of interior cell gid after the last step: after

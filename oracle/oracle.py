@@ -32,6 +32,25 @@ _P = C.c_void_p
 _I = C.c_int
 
 
+def reference_checkout() -> str | None:
+    """Root of a checkout of the reference (saleemayman/cavityflow_cuda): the
+    directory named by the environment variable LBM_REFERENCE_DIR, else a
+    directory ``reference`` beside this repository; None when neither exists
+    (as on a machine that only runs the prebuilt oracle files)."""
+    env = os.environ.get("LBM_REFERENCE_DIR")
+    cands = [env] if env else [os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.isdir(os.path.join(c, "src")):
+            return os.path.abspath(c)
+    return None
+
+
+def reference_src() -> str | None:
+    """The checkout's src/ directory, or None."""
+    root = reference_checkout()
+    return os.path.join(root, "src") if root else None
+
+
 def build(ref_src: str | None = None) -> None:
     """Build liblbm_oracle.so (always) and the reference harness when ``ref_src`` exists."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -95,21 +114,22 @@ class Oracle(_Lib):
         self.lib.orc_set_lid.argtypes = [_P, _I, _I, _I]
         self.lib.orc_set_lid(_ptr(flags), nx, ny, nz)
 
-    def alpha(self, dd, flags, inv_tau, lid_u, g=(0.0, 0.0, 0.0), origin=None, size=None):
+    def alpha(self, dd, flags, inv_tau, lid_u, g=(0.0, 0.0, 0.0), origin=None, size=None, wall=False):
+        """wall=True: the moving top wall (lid_u along x) instead of an injection lid."""
         nz, ny, nx = (s - 2 for s in flags.shape)
         origin = (0, 0, 0) if origin is None else origin
         size = (nx + 2, ny + 2, nz + 2) if size is None else size
         R = self._real(dd.dtype)
-        fn = self._fn("alpha", dd.dtype)
+        fn = self._fn("alpha_wall" if wall else "alpha", dd.dtype)
         fn.argtypes = [_P, _P, _I, _I, _I, R, R, R, R, R, _P, _P]
         fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, g[0], g[1], g[2], lid_u, _i3(origin), _i3(size))
 
-    def beta(self, dd, flags, inv_tau, lid_u, origin=None, size=None):
+    def beta(self, dd, flags, inv_tau, lid_u, origin=None, size=None, wall=False):
         nz, ny, nx = (s - 2 for s in flags.shape)
         origin = (0, 0, 0) if origin is None else origin
         size = (nx + 2, ny + 2, nz + 2) if size is None else size
         R = self._real(dd.dtype)
-        fn = self._fn("beta", dd.dtype)
+        fn = self._fn("beta_wall" if wall else "beta", dd.dtype)
         fn.argtypes = [_P, _P, _I, _I, _I, R, R, _P, _P]
         fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, _i3(origin), _i3(size))
 
@@ -141,21 +161,24 @@ class Oracle(_Lib):
         fn(_ptr(dd), _ptr(flags), nx, ny, nz, (C.c_int32 * 6)(*bc))
         return dd, flags
 
-    def step_s(self, dd, flags, counter, inv_tau, lid_u, kind, origin=None, size=None):
+    def step_s(self, dd, flags, counter, inv_tau, lid_u, kind, origin=None, size=None, wall=False):
         nz, ny, nx = (s - 2 for s in flags.shape)
         origin = (0, 0, 0) if origin is None else origin
         size = (nx + 2, ny + 2, nz + 2) if size is None else size
-        fn = self.lib.orc_beta_s if counter & 1 else self.lib.orc_alpha_s
+        w = "_wall" if wall else ""
+        fn = getattr(self.lib, f"orc_beta{w}_s" if counter & 1 else f"orc_alpha{w}_s")
         fn.argtypes = [_P, _P, _I, _I, _I, C.c_float, C.c_float, _I, _P, _P, C.c_uint32]
         fn(_ptr(dd), _ptr(flags), nx, ny, nz, inv_tau, lid_u, int(kind), _i3(origin), _i3(size),
            int(counter) & 0xFFFFFFFF)
 
     def run_cavity_s(self, nx, ny, nz, kind, inv_tau, lid_u, steps, lid=True):
+        """lid: True (the injection lid), "wall" (the moving top wall) or False."""
         dd, flags = self.init_s(nx, ny, nz)
-        if lid:
+        wall = lid == "wall"
+        if lid and not wall:
             self.set_lid(flags)
         for i in range(steps):
-            self.step_s(dd, flags, i, inv_tau, lid_u, kind)
+            self.step_s(dd, flags, i, inv_tau, lid_u, kind, wall=wall)
         return dd, flags
 
     def unshift(self, dd, kind):
@@ -217,18 +240,21 @@ class Oracle(_Lib):
             out[name] = raw[256 * i:256 * (i + 1)].split(b"\0", 1)[0].decode()
         return out
 
-    def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0)):
+    def step(self, dd, flags, counter, inv_tau, lid_u, g=(0.0, 0.0, 0.0), wall=False):
         if counter & 1:
-            self.beta(dd, flags, inv_tau, lid_u)
+            self.beta(dd, flags, inv_tau, lid_u, wall=wall)
         else:
-            self.alpha(dd, flags, inv_tau, lid_u, g)
+            self.alpha(dd, flags, inv_tau, lid_u, g, wall=wall)
 
     def run_cavity(self, nx, ny, nz, dtype, inv_tau, lid_u, steps, g=(0.0, 0.0, 0.0), lid=True):
+        """lid: True (the reference's injection lid), "wall" (the moving top
+        wall) or False (closed box at rest)."""
         dd, flags = self.init(nx, ny, nz, dtype)
-        if lid:
+        wall = lid == "wall"
+        if lid and not wall:
             self.set_lid(flags)
         for i in range(steps):
-            self.step(dd, flags, i, inv_tau, lid_u, g)
+            self.step(dd, flags, i, inv_tau, lid_u, g, wall=wall)
         return dd, flags
 
 

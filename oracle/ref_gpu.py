@@ -158,3 +158,53 @@ def momentum(dd: np.ndarray) -> np.ndarray:
                   [0, 0, 1], [0, 0, -1], [0, 0, 0]], dtype=np.float64)
     f = dd.astype(np.float64)
     return np.einsum("kd,kzyx->dzyx", c, f)
+
+
+_C = ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (1, 1, 0), (-1, -1, 0), (1, -1, 0), (-1, 1, 0), (1, 0, 1),
+      (-1, 0, -1), (1, 0, -1), (-1, 0, 1), (0, 1, 1), (0, -1, -1), (0, 1, -1), (0, -1, 1), (0, 0, 1), (0, 0, -1),
+      (0, 0, 0))
+
+
+def interior_momentum_max_diff(a, b) -> float:
+    """max over interior cells and components of |j_a - j_b|, j = sum_k c_k f_k
+    of the raw slots at each cell, for two reference-layout population tensors
+    on the device (19, nz+2, ny+2, nx+2); float64 accumulation one slot at a
+    time, so no host copy of the (possibly many-GB) arrays is needed."""
+    import torch
+
+    inner = (slice(1, -1),) * 3
+    worst = 0.0
+    for d in range(3):
+        acc = None
+        for k in range(19):
+            c = _C[k][d]
+            if c == 0:
+                continue
+            t = a[k][inner].double() - b[k][inner].double()
+            acc = c * t if acc is None else acc.add_(t, alpha=c)
+        worst = max(worst, float(acc.abs().max()))
+        del acc
+    torch.cuda.synchronize()
+    return worst
+
+
+def interior_momentum_max(a) -> float:
+    """max |j| over interior cells of a reference-layout tensor on the device."""
+    inner = (slice(1, -1),) * 3
+    worst = 0.0
+    for d in range(3):
+        acc = None
+        for k in range(19):
+            c = _C[k][d]
+            if c == 0:
+                continue
+            t = a[k][inner].double()
+            acc = c * t if acc is None else acc.add_(t, alpha=c)
+        worst = max(worst, float(acc.abs().max()))
+    return worst
+
+
+def interior_mass(a) -> float:
+    """FP64 sum of every slot over the interior cells of a device tensor."""
+    inner = (slice(None),) + (slice(1, -1),) * 3
+    return float(a[inner].double().sum())

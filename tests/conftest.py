@@ -27,9 +27,9 @@ def reference():
     """The reference's own CPU kernels; only where the reference checkout exists."""
     from oracle import oracle as orc
 
-    src = "/root/reference/src"
-    if not os.path.isdir(src):
-        pytest.skip("reference checkout not present")
+    src = orc.reference_src()
+    if src is None:
+        pytest.skip("reference checkout not present (LBM_REFERENCE_DIR)")
     orc.build(src)
     return orc.Reference()
 

@@ -218,7 +218,8 @@ def sha256(a: np.ndarray) -> str:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-src", default="/root/reference/src")
+    ap.add_argument("--ref-src", default=orc.reference_src(),
+                    help="the reference checkout's src/ (default: LBM_REFERENCE_DIR/src)")
     ap.add_argument("--skip-digests", action="store_true")
     ap.add_argument("--params-one", nargs=2, metavar=("XML", "DTYPE"))
     ap.add_argument("--config-one", nargs=2, metavar=("XML", "DTYPE"))

@@ -1,6 +1,7 @@
 """The C ABI library without a GPU: it loads, exports every declared entry
 point, derives lattice parameters exactly as the reference does, and reports
 errors as status codes."""
+import ctypes as C
 import glob
 import json
 import os
@@ -64,6 +65,7 @@ def test_status_strings_and_errors_without_device(lib):
     import torch
 
     from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmError
+    from cavityflow_cuda_gb300 import solver as solver_mod
 
     assert lib.lbm_status_string(0) == b"ok"
     assert b"bounds" in lib.lbm_status_string(2)
@@ -71,8 +73,17 @@ def test_status_strings_and_errors_without_device(lib):
         CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32", boundary=(1, 1, 1, 1, 1, 3))
     assert ei.value.status == 1  # invalid boundary flag, checked before any CUDA call
     with pytest.raises(LbmError) as ei:
-        CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32", fused_multiply_add=True)
-    assert ei.value.status == 1  # fused multiply-adds are an FP64 option
+        CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f16sr", fused_multiply_add=True)
+    assert ei.value.status == 1  # fused multiply-adds are an FP64 and FP32 option
+    with pytest.raises(LbmError) as ei:
+        CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32", lid="wall", boundary=(1, 1, 1, 2, 1, 1))
+    assert ei.value.status == 1  # a moving top wall needs an obstacle top face
+    p = solver_mod._Params()
+    p.size[:] = [8, 8, 8]
+    p.boundary[:] = [1] * 6
+    p.inv_tau, p.lid_mode = 1.6, 2
+    h = C.c_void_p()
+    assert lib.lbm_create(C.byref(p), C.byref(h)) == 1 and not h.value  # unknown lid mode
     if not torch.cuda.is_available():
         with pytest.raises(LbmError) as ei:
             CLbmSolverGB300((8, 8, 8), 1.6, 0.05)
@@ -117,10 +128,10 @@ def test_cli_usage_and_argument_errors(lib, tmp_path):
 
 
 def test_launch_variant_menu_size(lib):
-    """18 register variants (0-17) and 6 bulk-copy variants (18-23); the GPU
+    """22 register variants (0-21) and 6 bulk-copy variants (22-27); the GPU
     parity tests enumerate exactly these."""
-    assert lib.lbm_fast_variant_count() == 24
-    assert lib.lbm_register_variant_count() == 18
+    assert lib.lbm_fast_variant_count() == 28
+    assert lib.lbm_register_variant_count() == 22
 
 
 def test_batch_and_server_arguments_checked_before_the_device(lib):
@@ -160,7 +171,8 @@ def test_batch_and_server_arguments_checked_before_the_device(lib):
     (dict(inv_tau=float("inf")), 1),
     (dict(lid_velocity=float("nan")), 1),
     (dict(storage="f16s", gravity=(0.0, -1e-5, 0.0)), 5),   # gravity: F64 and F32 only
-    (dict(storage="f32", fused_multiply_add=True), 1),      # fused multiply-adds: F64 only
+    (dict(storage="bf16s", fused_multiply_add=True), 1),    # fused multiply-adds: F64 and F32 only
+    (dict(lid="wall", boundary=(1, 1, 1, 8, 1, 1)), 1),     # moving wall: the top face must be an obstacle
 ])
 def test_create_argument_checks_before_the_device(lib, kw, status):
     """lbm_create rejects bad parameters with a status code (the reference

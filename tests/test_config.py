@@ -12,6 +12,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN
+from oracle import oracle as orc
 
 CONFIGS = json.load(open(os.path.join(GOLDEN, "configs.json")))
 PARAMS = json.load(open(os.path.join(GOLDEN, "params.json")))
@@ -110,7 +111,8 @@ def test_reader_ignores_subdomain_num_as_the_serial_reference(lib, tmp_path):
     assert read_configuration(path)["subdomain_num"] == (1, 1, 1)
 
 
-REF_CONFIGS = "/root/reference/configurations"
+_REF = orc.reference_checkout()
+REF_CONFIGS = os.path.join(_REF, "configurations") if _REF else ""
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_CONFIGS), reason="reference checkout not present")

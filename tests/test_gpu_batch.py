@@ -30,7 +30,7 @@ def test_batch_domains_match_single_solvers(gpu, storage):
         assert np.array_equal(got[i].view(np.uint8), want.view(np.uint8)), (storage, i, size)
 
 
-@pytest.mark.parametrize("variant", range(18))
+@pytest.mark.parametrize("variant", range(22))
 def test_batch_every_variant(gpu, variant):
     from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmBatch
 

@@ -1,0 +1,192 @@
+"""The opt-in mass-conserving lid (lbm_params.lid_mode = LBM_LID_MOVING_WALL):
+the top face is a wall moving at U along x, the cells under it stay FLUID and
+take Ladd's moving-wall correction on the populations the wall sends back.
+
+Parity: bit-identical to the oracle's restatement (oracle/lbm_oracle_body.h
+wall_correct) for every launch variant and storage, on the flag-array path
+(an interior obstacle, cuboid steps) and through graph replays and
+checkpoints.  The mass criterion: FP64 mass of the 64^3 lid-driven cavity
+(lid 0.05, nu 0.032, Re 100) constant to 1e-10 relative over 1000 steps,
+where the reference's injection lid drifts by orders of magnitude more.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+KIND = {"f16s": 0, "bf16s": 1, "f16sr": 2}
+
+
+def wall_solver(n, storage, inv_tau, lid, **kw):
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    return CLbmSolverGB300(n, inv_tau, lid, storage=storage, lid="wall", **kw)
+
+
+def same_bits(a, b):
+    return a.shape == b.shape and np.array_equal(np.ascontiguousarray(a).view(np.uint8),
+                                                  np.ascontiguousarray(b).view(np.uint8))
+
+
+def oracle_run(oracle, n, storage, itau, lid, steps):
+    if storage in KIND:
+        dd, flags = oracle.run_cavity_s(*n, KIND[storage], itau, lid, steps, lid="wall")
+        return oracle.unshift(dd, KIND[storage]), flags
+    dtype = np.float64 if storage == "f64" else np.float32
+    return oracle.run_cavity(*n, dtype, itau, dtype(lid), steps, lid="wall")
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16s", "bf16s", "f16sr"])
+@pytest.mark.parametrize("variant", range(28))
+def test_moving_wall_matches_oracle_every_variant(gpu, oracle, storage, variant):
+    from cavityflow_cuda_gb300 import LbmError
+
+    dtype = np.float64 if storage == "f64" else np.float32
+    _, itau = orc.tau_of(0.032, dtype)
+    lid = float(dtype(0.07))
+    ran = 0
+    for n, steps in (((37, 9, 5), 13), ((300, 4, 3), 6), ((6, 7, 8), 11)):
+        want, _ = oracle_run(oracle, n, storage, itau, lid, steps)
+        try:
+            s = wall_solver(n, storage, itau, lid, fast_variant=variant)
+        except LbmError as e:  # a bulk-copy variant whose buffers exceed shared memory
+            assert e.status == 5
+            continue
+        with s:
+            info = s.info()
+            assert info["fast_path"] == 1 and info["lid_mode"] == 1 and info["moving_wall"] == 1
+            s.run(steps)
+            assert same_bits(s.get_all(), want), (storage, variant, n)
+            ran += 1
+    assert ran >= 2
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16sr"])
+def test_moving_wall_flag_array_path_and_cuboid_steps(gpu, oracle, storage):
+    """An interior obstacle sends the solver to the flag-array kernels; whole
+    steps and cuboid steps there match the oracle bit for bit."""
+    from cavityflow_cuda_gb300 import OBSTACLE
+
+    dtype = np.float64 if storage == "f64" else np.float32
+    _, itau = orc.tau_of(0.04, dtype)
+    lid = float(dtype(0.06))
+    n = (14, 11, 9)
+    kind = KIND.get(storage)
+    if kind is None:
+        dd, flags = oracle.init(*n, dtype)
+    else:
+        dd, flags = oracle.init_s(*n)
+    block = (slice(3, 5), slice(4, 7), slice(5, 8))  # z, y, x of the obstacle
+    flags[block] = orc.OBSTACLE
+    cub_o, cub_s = (2, 3, 1), (9, 9, 8)  # includes the row under the wall
+    with wall_solver(n, storage, itau, lid) as s:
+        s.setFlags(np.full((2, 3, 3), OBSTACLE, np.int32), (5, 4, 3), (3, 3, 2))
+        assert s.info()["fast_path"] == 0
+        for i in range(24):
+            o, sz = (cub_o, cub_s) if i >= 12 else (None, None)  # whole-domain steps, then cuboid steps
+            if kind is not None:
+                oracle.step_s(dd, flags, i, itau, lid, kind, origin=o, size=sz, wall=True)
+            elif i & 1:
+                oracle.beta(dd, flags, itau, dtype(lid), origin=o, size=sz, wall=True)
+            else:
+                oracle.alpha(dd, flags, itau, dtype(lid), origin=o, size=sz, wall=True)
+            (s.simulationStepBeta if i & 1 else s.simulationStepAlpha)(o, sz)
+        got = s.get_all()
+    want = dd if kind is None else oracle.unshift(dd, kind)
+    assert same_bits(got, want)
+
+
+def test_moving_wall_conserves_fp64_mass(gpu, oracle):
+    """64^3, lid 0.05, nu 0.032 (Re 100), 1000 steps: relative mass change
+    <= 1e-10 with the moving wall; the injection lid drifts far more."""
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    _, itau = orc.tau_of(0.032, np.float64)
+    n = (64, 64, 64)
+    drift = {}
+    for mode in ("wall", "injection"):
+        with CLbmSolverGB300(n, itau, 0.05, storage="f64", lid=mode) as s:
+            m0 = s.reduce()
+            s.run(1000)
+            m1 = s.reduce()
+            jmax = np.abs(s.getVelocities()[0]).max()
+        drift[mode] = abs(m1[0] - m0[0]) / m0[0]
+        assert jmax > 0.01, mode  # the lid drives the flow
+        if mode == "wall":
+            assert m1[1] > 0.0  # x momentum put in by the moving wall
+    print(f"\nrelative FP64 mass change over 1000 steps: moving wall {drift['wall']:.3e}, "
+          f"injection lid {drift['injection']:.3e}")
+    assert drift["wall"] <= 1e-10
+    assert drift["injection"] > 1e3 * max(drift["wall"], 1e-16)
+
+
+def test_moving_wall_mass_matches_oracle(gpu, oracle):
+    """The reduction of a moving-wall run equals the oracle's."""
+    _, itau = orc.tau_of(0.032, np.float64)
+    n, steps = (20, 18, 16), 301
+    want, flags = oracle.run_cavity(*n, np.float64, itau, 0.05, steps, lid="wall")
+    with wall_solver(n, "f64", itau, 0.05) as s:
+        s.run(steps)
+        got = s.reduce()
+    np.testing.assert_allclose(got, oracle.reduce(want, flags, last_was_alpha=True), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16sr"])
+def test_moving_wall_graphs_checkpoints_and_late_start(gpu, oracle, storage, tmp_path):
+    """Graph replays equal single steps; a wall set moving after some steps at
+    rest (the graph captured before is dropped) equals the oracle; a
+    checkpoint written mid-run resumes bit-identically with the wall moving."""
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    _, itau = orc.tau_of(0.02, np.float32)
+    lid = 0.05
+    n = (24, 20, 16)
+    with wall_solver(n, storage, itau, lid) as a, wall_solver(n, storage, itau, lid) as b:
+        a.run(260)
+        for i in range(260):
+            (b.simulationStepBeta if i & 1 else b.simulationStepAlpha)()
+        assert same_bits(a.get_all(), b.get_all())
+        path = str(tmp_path / "w.ckpt")
+        a.save_checkpoint(path)
+        a.run(130)
+        with CLbmSolverGB300.from_checkpoint(path) as c:
+            assert c.info()["lid_mode"] == 1 and c.info()["moving_wall"] == 1
+            c.run(130)
+            assert same_bits(a.get_all(), c.get_all())
+    # at rest for 140 steps (a graph is captured), then the wall starts
+    with CLbmSolverGB300(n, itau, lid, storage=storage, lid="wall", driven_cavity=False) as s:
+        assert s.info()["moving_wall"] == 0
+        s.run(140)
+        s.setDrivenCavity()
+        assert s.info()["moving_wall"] == 1
+        s.run(140)
+        got = s.get_all()
+    kind = KIND.get(storage)
+    if kind is None:
+        dd, flags = oracle.init(*n, np.float32)
+        for i in range(280):
+            oracle.step(dd, flags, i, itau, np.float32(lid if i >= 140 else 0.0), wall=i >= 140)
+        want = dd
+    else:
+        dd, flags = oracle.init_s(*n)
+        for i in range(280):
+            oracle.step_s(dd, flags, i, itau, lid if i >= 140 else 0.0, kind, wall=i >= 140)
+        want = oracle.unshift(dd, kind)
+    assert same_bits(got, want)
+
+
+def test_checkpoint_lid_mode_must_match(gpu, tmp_path):
+    from cavityflow_cuda_gb300 import LbmError
+
+    path = str(tmp_path / "w.ckpt")
+    with wall_solver((8, 8, 8), "f32", 1.6, 0.05) as s:
+        s.run(3)
+        s.save_checkpoint(path)
+    from cavityflow_cuda_gb300 import CLbmSolverGB300
+
+    with CLbmSolverGB300((8, 8, 8), 1.6, 0.05, storage="f32") as t:
+        with pytest.raises(LbmError) as ei:
+            t.load_checkpoint(path)
+        assert ei.value.status == 1

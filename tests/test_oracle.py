@@ -117,6 +117,38 @@ def test_lid_changes_mass(oracle):
     assert abs(oracle.reduce(dd, flags, last_was_alpha=True)[0] - m0) > 1e-9 * m0
 
 
+def test_moving_wall_conserves_mass_and_drives_the_flow(oracle):
+    """The opt-in moving top wall: every cell under it gets -U/6 on population
+    5 and +U/6 on population 6, so FP64 mass stays at its initial value to
+    rounding while the lid drives a flow in +x under it, and the x momentum
+    the wall puts in grows the total."""
+    _, itau = orc.tau_of(0.032, np.float64)
+    n = (12, 10, 9)
+    dd, flags = oracle.init(*n, np.float64)
+    m0 = oracle.reduce(dd, flags, last_was_alpha=False)[0]
+    for i in range(200):
+        oracle.step(dd, flags, i, itau, 0.08, wall=True)
+    out = oracle.reduce(dd, flags, last_was_alpha=False)
+    assert abs(out[0] - m0) <= 1e-13 * m0
+    assert out[1] > 0.01
+    rho, jx, _, _ = oracle.macros(dd, flags, last_was_alpha=False, lid_u=0.08)
+    assert (jx[1:-1, n[1], 1:-1] > 0.01).all()  # the row under the wall moves with it
+    assert (flags[1:-1, 1:-1, 1:-1] == orc.FLUID).all()  # no injection cells
+
+
+@pytest.mark.parametrize("kind", [0, 2])
+def test_moving_wall_16bit_tracks_fp32(oracle, kind):
+    """The same wall on shifted 16-bit storage stays within the storage's
+    rounding of the FP32 run."""
+    _, itau = orc.tau_of(0.032, np.float32)
+    n, steps = (10, 9, 8), 60
+    ref, flags = oracle.run_cavity(*n, np.float32, itau, np.float32(0.08), steps, lid="wall")
+    dd, _ = oracle.run_cavity_s(*n, kind, itau, 0.08, steps, lid="wall")
+    got = oracle.unshift(dd, kind)
+    inner = (slice(None), slice(1, -1), slice(1, -1), slice(1, -1))
+    assert np.abs(got[inner] - ref[inner]).max() < 2e-4
+
+
 def test_macros_of_lid_and_walls(oracle):
     _, itau = orc.tau_of(0.032, np.float64)
     dd, flags = oracle.run_cavity(6, 5, 4, np.float64, itau, 0.07, 9)
