@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--batch-storages", default="f32,f16s,f16sr", help="storages of --workload batch / serve")
     ap.add_argument("--batch-variant", type=int, default=-1,
                     help="register variant of --workload batch (default: autotuned per storage)")
+    ap.add_argument("--batch-single-size", type=int, default=384,
+                    help="--workload batch: edge of the single-domain comparison cavity (0: none)")
     ap.add_argument("--precision-size", type=int, default=512)
     ap.add_argument("--precision-steps", type=int, default=5000)
     ap.add_argument("--serve-count", type=int, default=10000)
@@ -567,10 +569,14 @@ def extensions(a):
         out["moving_wall"] = moving_wall_measure()
     except Exception as e:
         out["moving_wall_error"] = repr(e)
+    single = {}
     try:
         ref = batch_reference_fields(a.batch_count, 4 + a.batch_steps)
         for st in ("f32", "f16s", "f16sr"):
-            out[f"batch_{st}"] = batch_measure(st, a.batch_count, a.batch_steps, ref_fields=ref)
+            out[f"batch_{st}"] = r = batch_measure(st, a.batch_count, a.batch_steps, ref_fields=ref)
+            single[st] = round(single_measure(st, 384, 400), 1)
+            r["single_domain_384_mlups"] = single[st]
+            r["batch_over_single"] = round(r["mlups"] / single[st], 3)
         del ref
         out["batch_note"] = (f"batched MLUPS over the seeded {a.batch_count}-cavity workload, {a.batch_steps} "
                              "steps; velocity errors against the same batch in FP64; compare with "
@@ -579,7 +585,9 @@ def extensions(a):
         out["batch_error"] = repr(e)
     try:
         for st in ("f32", "f16sr"):
-            out[f"serve_{st}"] = serve_measure(st, a.serve_count, a.serve_step_scale, l2_sample=16)
+            out[f"serve_{st}"] = r = serve_measure(st, a.serve_count, a.serve_step_scale, l2_sample=16)
+            if st in single:
+                r["busy_over_single"] = round(r["busy_mlups"] / single[st], 3)
         out["serve_note"] = (f"the seeded {a.serve_count}-request stream at 200 req/s, steps U[500,20000] scaled "
                              f"by {a.serve_step_scale}, 150 GB budget")
     except Exception as e:
@@ -598,9 +606,11 @@ def main():
         torch.cuda.set_device(0)
         storages = a.batch_storages.split(",")
         res = {s: batch_measure(s, a.batch_count, a.batch_steps, variant=a.batch_variant) for s in storages}
-        for s in storages:
-            res[s]["single_domain_384_mlups"] = round(single_measure(s, 384, 400), 1)
-            res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s]["single_domain_384_mlups"], 3)
+        if a.batch_single_size > 0:
+            n = a.batch_single_size
+            for s in storages:
+                res[s][f"single_domain_{n}_mlups"] = round(single_measure(s, n, 400), 1)
+                res[s]["batch_over_single"] = round(res[s]["mlups"] / res[s][f"single_domain_{n}_mlups"], 3)
         print(json.dumps({"workload": "batch", "results": res}), flush=True)
         return
     if a.workload == "serve":

@@ -321,6 +321,8 @@ int lbm_batch_set_fast_variant(lbm_batch* b, int32_t variant)
     if (!b) return fail(LBM_ERR_INVALID_ARGUMENT, "batch is NULL");
     if (variant < 0 || variant >= lbm::kRegisterVariants)
         return fail(LBM_ERR_INVALID_ARGUMENT, "batch variant %d not in [0, %d)", variant, lbm::kRegisterVariants);
+    if (!b->views.empty() && !lbm::fast_variant_fits(b->storage, variant, b->views[0]->g))
+        return fail(LBM_ERR_UNSUPPORTED, "variant %d's vectors do not fit the batch's packed rows", variant);
     CK(cudaSetDevice(b->device), "cudaSetDevice");
     b->variant = variant;
     for (lbm_solver* v : b->views) v->variant = variant;
@@ -347,6 +349,10 @@ int lbm_batch_autotune(lbm_batch* b, int32_t pairs, int32_t* best, float* ms_per
     if (e == cudaSuccess && b->last_alpha) e = batch_launch(b, b->variant, false, st, 0);
     int r = LBM_OK;
     for (int v = 0; v < lbm::kRegisterVariants && e == cudaSuccess && r == LBM_OK; ++v) {
+        if (!lbm::fast_variant_fits(b->storage, v, b->views[0]->g)) {  // vectors wider than the packed rows
+            if (ms_per_pair) ms_per_pair[v] = -1.f;
+            continue;
+        }
         b->variant = v;
         if ((r = build_table(b))) break;
         for (int i = 0; i < 1 + pairs && e == cudaSuccess; ++i) {  // first pair warms up

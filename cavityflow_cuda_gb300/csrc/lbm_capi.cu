@@ -87,18 +87,16 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // (one cell).
 }  // namespace
 
-// Batches of the seeded 512-cavity workload (edges 16..96) favour two-warp
-// alpha blocks with the block-wide beta exchange: FP32 16-byte vectors in both
-// kernels (variant 11), FP16 a 16-byte alpha with an 8-byte four-warp beta
-// (variant 12), FP16 with stochastic rounding 8-byte vectors in four-warp
-// blocks (variant 9).
+// Batch and server rows are packed for 8-byte vectors (kPackedX1Align), so
+// their variants use 8-byte (or narrower) vectors in both kernels: the direct
+// FP32 beta (variant 13), the packed 16-bit beta (22), and the FP64 warp
+// exchange (3).
 int lbm_detail::default_batch_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F64: return 3;
-    case LBM_STORAGE_F16S: return 12;
-    case LBM_STORAGE_F16SR: return 9;
-    default: return 11;
+    case LBM_STORAGE_F32: return 13;
+    default: return 22;
     }
 }
 
@@ -106,9 +104,9 @@ int lbm_detail::default_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F32: return 13;
-    case LBM_STORAGE_F16S: return 18;
+    case LBM_STORAGE_F16S: return 20;
     case LBM_STORAGE_BF16S: return 18;
-    case LBM_STORAGE_F16SR: return 18;
+    case LBM_STORAGE_F16SR: return 19;
     default: return 3;
     }
 }

@@ -61,17 +61,19 @@ __host__ __device__ constexpr T weight(int k)
 // access right of the last group and is a multiple of 32 bytes, and every
 // slot starts on a 256-byte boundary.
 //
-// Batches and servers pack their boxes' rows tighter (x1_align = 16): x = 1
-// on a 16-byte boundary and P a multiple of 16 bytes.  L2 fetches a 128-byte
-// line whole when a short row touches part of it; with packed rows the
-// neighbouring rows' cells fill more of those lines.  The register kernels
-// only need x = 1 on a 16-byte boundary and index through idx(), so both
-// layouts run the same code with the same results; the bulk-copy kernels run
-// on the default layout only.
+// Batches and servers pack their boxes' rows tighter (x1_align = 8): x = 1
+// on an 8-byte boundary, rows sized for 8-byte vectors and P a multiple of 8
+// bytes.  L2 fetches a 128-byte line whole when a short row touches part of
+// it; with packed rows the neighbouring rows' cells fill more of those lines,
+// and the rows of small boxes carry less padding.  The register kernels need
+// x = 1 aligned to their widest vector and index through idx(), so every
+// layout runs the same code with the same results for the variants whose
+// vectors fit it (vector_fits); the bulk-copy kernels run on the default
+// layout only.
 // ---------------------------------------------------------------------------
 struct Grid {
     int nx, ny, nz;      // interior cells
-    int V;               // cells per 16-byte vector
+    int V;               // cells per widest vector the rows are sized for (16 bytes; 8 when packed)
     int xoff;            // column of halo cell x = 0
     int G;               // vector groups per row, ceil(nx / V)
     long long P;         // row pitch (elements)
@@ -91,12 +93,13 @@ struct Grid {
     __host__ __device__ long long cells() const { return (long long)(nx + 2) * (ny + 2) * (nz + 2); }
 };
 
+// x1_align: byte alignment of x = 1, 32 (the default layout), 16 or 8.
 inline Grid make_grid(int nx, int ny, int nz, int elem_bytes, int x1_align = 32)
 {
     Grid g;
     g.nx = nx; g.ny = ny; g.nz = nz;
-    g.V = 16 / elem_bytes;
-    const int sector = (x1_align == 16 ? 16 : 32) / elem_bytes;
+    g.V = (x1_align < 16 ? x1_align : 16) / elem_bytes;
+    const int sector = x1_align / elem_bytes;
     g.xoff = sector - 1;
     g.G = (nx + g.V - 1) / g.V;
     const long long need = (long long)g.xoff + (long long)g.G * g.V + 2;  // last scalar column + 1
@@ -108,10 +111,14 @@ inline Grid make_grid(int nx, int ny, int nz, int elem_bytes, int x1_align = 32)
 }
 
 // Alignment of x = 1 in the rows of batch and server boxes (see above).
-constexpr int kPackedX1Align = 16;
+constexpr int kPackedX1Align = 8;
 
 // True for the default layout (x = 1 on a 32-byte boundary).
 inline bool default_layout(const Grid& g, int elem_bytes) { return g.xoff == 32 / elem_bytes - 1; }
+
+// Whether vectors of `bytes` bytes are aligned in this layout and its rows
+// have room for them.
+inline bool vector_fits(const Grid& g, int elem_bytes, int bytes) { return bytes <= g.V * elem_bytes; }
 
 // ---------------------------------------------------------------------------
 // Storage types.  F64/F32 hold f_i; F16S/BF16S/F16SR hold the deviation

@@ -436,8 +436,9 @@ __device__ __forceinline__ void beta_cells_direct(typename St::bits* __restrict_
 // cells), or the aligned vector that holds all but one of the window's
 // elements plus that one element (2 accesses; the extra bytes come from the
 // same L1 sectors).  Stores always use the window's pieces, since the aligned
-// vector's other element belongs to the neighbouring group.  Rows whose last
-// group is partial take beta_cells_direct for that group.
+// vector's other element belongs to the neighbouring group.  In a row's last
+// group, cells past the row's end skip the collision and store back exactly
+// what they read, so partial groups run the same code.
 // ---------------------------------------------------------------------------
 constexpr int kPkMaxWords = 5;
 
@@ -529,26 +530,31 @@ __device__ __forceinline__ float pk_in(uint32_t w, int hi)
     else return __half2float(__ushort_as_half((unsigned short)(hi ? (w >> 16) : (w & 0xffffu))));
 }
 
-// Step results rounded to 16-bit patterns: one alone, or two packed (lo, hi)
-// by one paired conversion with the same rounding as the single one.
+// A step result as the float its store converts: for stochastic rounding
+// with the population's dither added below the bits half precision drops
+// (store_sr), otherwise unchanged.
 template <class St>
-__device__ __forceinline__ uint32_t pk_one(float v, uint32_t h, int k)
+__device__ __forceinline__ float pk_pre(float v, uint32_t h, int k)
 {
-    return (uint32_t)store_pop<St>(v, h, k);
+    if constexpr (St::stochastic) return __uint_as_float(__float_as_uint(v) + sr_dither(h, k));
+    else return v;
+}
+// Such floats rounded to 16-bit patterns: one alone (low half), or two packed
+// (lo, hi) by one paired conversion with the same rounding as the single one.
+// A 16-bit value read as a float and not dithered comes back exactly.
+template <class St>
+__device__ __forceinline__ uint32_t pk_one(float d)
+{
+    if constexpr (St::stochastic) return (uint32_t)__half_as_ushort(__float2half_rz(d));
+    else return (uint32_t)St::store(d);
 }
 template <class St>
-__device__ __forceinline__ uint32_t pk_two(float lo, float hi, uint32_t hlo, uint32_t hhi, int k)
+__device__ __forceinline__ uint32_t pk_two(float lo, float hi)
 {
     uint32_t r;
-    if constexpr (St::stochastic) {
-        const float a = __uint_as_float(__float_as_uint(hi) + sr_dither(hhi, k));
-        const float b = __uint_as_float(__float_as_uint(lo) + sr_dither(hlo, k));
-        asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(a), "f"(b));
-    } else if constexpr (std::is_same<St, BF16S>::value) {
-        asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
-    } else {
-        asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
-    }
+    if constexpr (St::stochastic) asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    else if constexpr (std::is_same<St, BF16S>::value) asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    else asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
     return r;
 }
 
@@ -562,10 +568,7 @@ __device__ __forceinline__ void beta_cells_pk(typename St::bits* __restrict__ dd
     if (!c.active) return;
     const int gi = c.gi, y = c.y, z = c.z;
     const int x0 = 1 + gi * CPT;
-    if (x0 + CPT - 1 > g.nx) {  // the row's last, partial group
-        beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, step);
-        return;
-    }
+    const int nvalid = g.nx - x0 + 1;  // cells of the group inside the row (a row's last group may be partial)
     const long long base = g.idx(x0, y, z);
     uint32_t w[Q][kPkMaxWords];
     static_for<0, Q>([&](auto kc) {
@@ -578,28 +581,37 @@ __device__ __forceinline__ void beta_cells_pk(typename St::bits* __restrict__ dd
     const float du = wall_shift<St>(lid_u);
     const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
     float pend[Q];
-    uint32_t hprev = 0;
     static_for<0, CPT>([&](auto vc) {
         constexpr int v = decltype(vc)::value;
+        const bool valid = v < nvalid;
         float cc[Q];
         static_for<0, Q>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
             using P = PkSlot<CPT, dir_x(k)>;
             cc[opp(k)] = pk_in<St>(w[k][P::in_word(v, kVec)], P::in_half(v, kVec));
         });
-        if (wall) wall_correct(cc, du);
-        if (lid) inject_step<St>(cc, 0.0f, lid_u);
-        else collide<St>(cc, inv_tau);
+        if (valid) {
+            if (wall) wall_correct(cc, du);
+            if (lid) inject_step<St>(cc, 0.0f, lid_u);
+            else collide<St>(cc, inv_tau);
+        } else {  // a cell past the row's end: every slot gets back the value read from it
+#pragma unroll
+            for (int k = 0; k < Q - 1; k += 2) {
+                const float t = cc[k];
+                cc[k] = cc[k + 1];
+                cc[k + 1] = t;
+            }
+        }
         uint32_t h = 0;
         if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
         static_for<0, Q>([&](auto kc) {
             constexpr int k = decltype(kc)::value;
             using P = PkSlot<CPT, dir_x(k)>;
-            if constexpr (P::single(v)) w[k][P::word(v)] = pk_one<St>(cc[k], h, k);
-            else if constexpr (P::first(v)) pend[k] = cc[k];
-            else w[k][P::word(v)] = pk_two<St>(pend[k], cc[k], hprev, h, k);
+            const float d = valid ? pk_pre<St>(cc[k], h, k) : cc[k];
+            if constexpr (P::single(v)) w[k][P::word(v)] = pk_one<St>(d);
+            else if constexpr (P::first(v)) pend[k] = d;
+            else w[k][P::word(v)] = pk_two<St>(pend[k], d);
         });
-        hprev = h;
     });
     static_for<0, Q>([&](auto kc) {
         constexpr int k = decltype(kc)::value;

@@ -457,7 +457,13 @@ cudaError_t launch_check_cavity(const uint8_t* flags, const Grid& g, unsigned lo
 bool fast_variant_fits(int storage, int variant, const Grid& g)
 {
     if (variant < 0 || variant >= kFastVariantCount) return false;
-    if (variant < kRegisterVariants) return true;
+    if (variant < kRegisterVariants) {  // both kernels' vectors aligned in this layout
+        const int eb = storage_elem_bytes(storage);
+        const int widest = 16 / (kFastMenu[variant].alpha.cpt_div < kFastMenu[variant].beta.cpt_div
+                                     ? kFastMenu[variant].alpha.cpt_div
+                                     : kFastMenu[variant].beta.cpt_div);
+        return vector_fits(g, eb, widest < eb ? eb : widest);
+    }
     const TmaConfig c = kTmaMenu[variant - kRegisterVariants];
     const int elem = storage_elem_bytes(storage);
     if (!default_layout(g, elem)) return false;  // the bulk-copy kernels run on the default layout only

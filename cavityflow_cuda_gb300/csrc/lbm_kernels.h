@@ -71,7 +71,7 @@ struct FastVariant {
     bool direct = false;
     int packed = 0;
 };
-constexpr int kRegisterVariants = 22;
+constexpr int kRegisterVariants = 24;
 constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
     {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
@@ -95,6 +95,8 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 64, 4}, {2, 64, 8}, false, true, 1},   // the same, <= 128 registers
     {{1, 64, 4}, {2, 64, 10}, false, true, 2},  // alpha 16-byte; beta 8-byte packed, vector loads
     {{1, 64, 4}, {2, 64, 8}, false, true, 2},   // the same, <= 128 registers
+    {{2, 64, 8}, {2, 64, 10}, false, true, 1},  // 8-byte alpha and packed beta (fit the packed batch rows)
+    {{2, 64, 8}, {2, 64, 10}, false, true, 2},  // the same, vector loads
 };
 struct TmaConfig {
     int rows;            // rows per work unit
@@ -119,7 +121,8 @@ inline int storage_elem_bytes(int storage)
 }
 cudaError_t launch_fast_step(int storage, int variant, bool alpha, void* dd, const Grid& g, const Params& p,
                              int lid_y, int* err, cudaStream_t st);
-// Whether a variant fits this domain (shared memory of the bulk-copy kernels).
+// Whether a variant fits this domain: its vectors' alignment in the domain's
+// row layout (register variants), shared memory (bulk-copy variants).
 bool fast_variant_fits(int storage, int variant, const Grid& g);
 // Cells per thread and threads per block of a variant's alpha or beta kernel
 // (for a row of nx cells).

@@ -370,6 +370,11 @@ int lbm_server_create(const lbm_server_config* cfg, lbm_server** out)
     s->cfg.max_round_steps &= ~1;
     s->variant = cfg->fast_variant > 0 && cfg->fast_variant <= lbm::kRegisterVariants ? cfg->fast_variant - 1
                                                                                        : default_batch_variant(cfg->storage);
+    const int32_t probe[3] = {8, 8, 8};  // any box: the packed rows' alignment does not depend on its size
+    if (!lbm::fast_variant_fits(cfg->storage, s->variant, request_grid(probe, cfg->storage))) {
+        delete s;
+        return fail(LBM_ERR_UNSUPPORTED, "variant %d's vectors do not fit the server's packed rows", s->variant);
+    }
     s->arena_bytes = (size_t)((double)cfg->budget_bytes * kArenaShare) / kAlign * kAlign;
     if (s->arena_bytes + (size_t)(1 << 30) > free_b) {
         delete s;

@@ -8,7 +8,11 @@
  * lattice parameters (tau, 1/tau, dimensionless lid velocity and gravity)
  * come from the reference's constructor unchanged, and it offers every
  * overload CLbmSolverGPU<T> offers, with the same argument meaning.
- * Link the program with liblbm_gb300.so.  See INTEGRATION.md.
+ * Link the program with liblbm_gb300.so.  The lid is the reference's
+ * VELOCITY_INJECTION plane, marked by the caller through setFlags as
+ * CController does; an optional last constructor argument
+ * LBM_LID_MOVING_WALL selects the mass-conserving moving top wall instead,
+ * which starts moving at construction.
  *
  * Error behaviour follows the reference: a failing CUDA call prints the error
  * and exits with its code (GPU_ERROR_CHECK, src/common.h:73-90); a cuboid
@@ -48,7 +52,7 @@ private:
 
 public:
     CLbmSolverGB300(int id, CDomain<T>& domain, std::vector<Flag> boundaryConditions,
-                    CConfiguration<T>* configuration)
+                    CConfiguration<T>* configuration, int lidMode = LBM_LID_INJECTION)
         : CLbmSolver<T>(id, domain, boundaryConditions, configuration), solver(NULL)
     {
         int numOfGPUsPerNode = 0;
@@ -63,7 +67,9 @@ public:
         p.lid_velocity = this->velocityDimLess[0];
         for (int d = 0; d < 3; ++d) p.gravity[d] = this->accelerationDimLess[d];
         p.device = this->id % numOfGPUsPerNode;  // src/CLbmSolverGPU.cu:42-45
+        p.lid_mode = lidMode;
         check(lbm_create(&p, &solver), "CLbmSolverGB300()");
+        if (lidMode == LBM_LID_MOVING_WALL) check(lbm_set_driven_cavity(solver), "CLbmSolverGB300()");
     }
 
     ~CLbmSolverGB300() { lbm_destroy(solver); }

@@ -213,7 +213,8 @@ typedef struct lbm_info {
     int32_t size[3];            /* interior cells                              */
     int32_t storage;
     int32_t value_size;         /* bytes per host value (4 or 8)               */
-    int32_t vector_cells;       /* cells per 16-byte vector of the fast path   */
+    int32_t vector_cells;       /* cells per widest vector the rows are sized
+                                   for: 16 bytes, 8 in batch and server rows  */
     int64_t step_counter;       /* steps taken (alpha on even, beta on odd)    */
     int32_t last_step_was_alpha;
     int32_t fast_path;          /* 1: flags match the box cavity, so the
@@ -234,7 +235,7 @@ typedef struct lbm_info {
     int64_t slot_stride;        /* elements per population slot                */
     int64_t device_bytes;       /* bytes of device memory the solver holds     */
     int64_t x1_column;          /* column of interior cell x = 1 in a row: 32
-                                   bytes in (the default), or 16 for the
+                                   bytes in (the default), or 8 for the
                                    packed rows of batch domains               */
     int32_t lid_mode;           /* lbm_params.lid_mode                         */
     int32_t moving_wall;        /* 1 while the top wall moves (moving-wall
@@ -308,11 +309,11 @@ int lbm_selftest_bounded_wait(lbm_solver* solver, int32_t limit_us);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: 22 register-blocked
- * vector kernels (0..21: cells per thread, threads per block and blocks per
+/* Number of launch variants of the box-cavity kernels: 24 register-blocked
+ * vector kernels (0..23: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
- * elements per warp, per block or not at all; 18..21 keep 16-bit populations
- * two cells per register) and 6 row-pipelined bulk-copy kernels (22..27: rows
+ * elements per warp, per block or not at all; 18..23 keep 16-bit populations
+ * two cells per register) and 6 row-pipelined bulk-copy kernels (24..29: rows
  * per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Number of register variants (the first variants; the batch kernel's menu). */
@@ -461,11 +462,15 @@ int lbm_batch_get_info(const lbm_batch* batch, lbm_batch_info* info);
 int lbm_batch_domain(lbm_batch* batch, int32_t index, lbm_solver** view);
 /* `steps` steps of every domain (alpha on even counters, beta on odd). */
 int lbm_batch_run(lbm_batch* batch, int64_t steps, void* stream);
-/* Selects a launch variant (a register variant) for the batch kernel. */
+/* Selects a launch variant (a register variant whose vectors are at most 8
+ * bytes wide, since batch rows are packed for them; LBM_ERR_UNSUPPORTED
+ * otherwise) for the batch kernel. */
 int lbm_batch_set_fast_variant(lbm_batch* batch, int32_t variant);
 /* Times each register variant on the whole batch (`pairs` alpha/beta pairs,
  * CUDA events), keeps the fastest and restores the populations.  ms_per_pair
- * (optional) receives lbm_register_variant_count() times.  Synchronous. */
+ * (optional) receives lbm_register_variant_count() times, -1 for a variant
+ * whose vectors are wider than the batch's packed rows (8 bytes).
+ * Synchronous. */
 int lbm_batch_autotune(lbm_batch* batch, int32_t pairs, int32_t* best, float* ms_per_pair);
 
 /* ---- servers: cavity-solve requests with continuous batching ---------------
@@ -486,7 +491,8 @@ typedef struct lbm_server_config {
     int32_t device;
     int32_t max_round_steps;    /* upper bound on steps per round (even)       */
     int32_t target_round_ms;    /* rounds sized to about this long; 0: fixed   */
-    int32_t fast_variant;       /* 0: default; v + 1: register variant v       */
+    int32_t fast_variant;       /* 0: default; v + 1: register variant v with
+                                   vectors of at most 8 bytes                  */
     int32_t reserved;
     int64_t budget_bytes;       /* device memory the server may hold           */
 } lbm_server_config;

@@ -1,7 +1,7 @@
 """The padded population layout (make_grid in csrc/lbm_core.cuh), checked on
-the CPU for both row layouts (the default 32-byte one and the packed 16-byte
-one of batches and servers) and every storage width: the invariants the
-vectorised kernels' memory accesses rely on."""
+the CPU for every row layout (the default 32-byte one, a 16-byte one and the
+packed 8-byte one of batches and servers) and every storage width: the
+invariants the vectorised kernels' memory accesses rely on."""
 import os
 import shutil
 import subprocess
@@ -19,7 +19,7 @@ int main()
 {
     int bad = 0;
     const int widths[3] = {2, 4, 8};
-    const int aligns[2] = {16, 32};
+    const int aligns[3] = {8, 16, 32};
     for (int eb : widths)
         for (int al : aligns)
             for (int nx = 1; nx <= 300; ++nx)
@@ -33,7 +33,11 @@ int main()
                     if ((g.P * eb) %% al != 0) { printf("pitch eb=%%d al=%%d nx=%%d\n", eb, al, nx); ++bad; }
                     // the last vector, and a window shifted one cell right of it, stay in the row
                     if (last + 1 > g.P - 1) { printf("room eb=%%d al=%%d nx=%%d\n", eb, al, nx); ++bad; }
-                    if ((long long)g.G * g.V < nx || g.V * eb != 16) { printf("groups eb=%%d nx=%%d\n", eb, nx); ++bad; }
+                    // rows sized for vectors as wide as x = 1's alignment (16 bytes at most)
+                    if ((long long)g.G * g.V < nx || g.V * eb != (al < 16 ? al : 16)) { printf("groups eb=%%d nx=%%d\n", eb, nx); ++bad; }
+                    // a variant's vectors fit exactly when they are no wider than that
+                    for (int vb = 2; vb <= 16; vb *= 2)
+                        if (vb >= eb && lbm::vector_fits(g, eb, vb) != (vb <= (al < 16 ? al : 16))) { printf("fits eb=%%d al=%%d vb=%%d\n", eb, al, vb); ++bad; }
                     if (g.PY != g.P * (ny + 2)) { printf("plane eb=%%d nx=%%d\n", eb, nx); ++bad; }
                     if ((g.S * eb) %% 256 != 0 || g.S < g.PY * (nz + 2)) { printf("slot eb=%%d al=%%d nx=%%d\n", eb, al, nx); ++bad; }
                     if (lbm::default_layout(g, eb) != (al == 32)) { printf("default eb=%%d al=%%d\n", eb, al); ++bad; }
