@@ -88,15 +88,15 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 }  // namespace
 
 // Batch and server rows are packed for 8-byte vectors (kPackedX1Align), so
-// their variants use 8-byte (or narrower) vectors in both kernels: the direct
-// FP32 beta (variant 13), the packed 16-bit beta (22), and the FP64 warp
-// exchange (3).
+// their variants use 8-byte (or narrower) vectors in both kernels.  On the
+// seeded 512-cavity workload the direct beta windows in two-warp blocks
+// (variant 13) are fastest for FP32 and the FP16 storages, the FP64 warp
+// exchange (3) for FP64.
 int lbm_detail::default_batch_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F64: return 3;
-    case LBM_STORAGE_F32: return 13;
-    default: return 22;
+    default: return 13;
     }
 }
 
@@ -105,8 +105,8 @@ int lbm_detail::default_variant(int storage)
     switch (storage) {
     case LBM_STORAGE_F32: return 13;
     case LBM_STORAGE_F16S: return 20;
-    case LBM_STORAGE_BF16S: return 18;
-    case LBM_STORAGE_F16SR: return 19;
+    case LBM_STORAGE_BF16S: return 20;
+    case LBM_STORAGE_F16SR: return 20;
     default: return 3;
     }
 }

@@ -65,7 +65,7 @@ def test_batch_views_getters_and_guards(gpu):
             assert np.array_equal(v.getVelocities(), s.getVelocities())
             assert np.allclose(v.reduce(), s.reduce(), rtol=1e-12)
         best, ms = b.autotune(pairs=2)
-        assert 0 <= best < 18 and b.info()["step_counter"] == 10
+        assert 0 <= best < 24 and b.info()["step_counter"] == 10
         v.simulationStepAlpha()          # a domain leaves the batch's time level
         with pytest.raises(LbmError):
             b.run(2)
@@ -74,9 +74,9 @@ def test_batch_views_getters_and_guards(gpu):
 
 @pytest.mark.parametrize("storage", ["f32", "f16sr", "f64"])
 def test_batch_packed_rows(gpu, storage):
-    """Batch domains pack their rows (x = 1 on a 16-byte boundary, 16-byte
-    row pitch) while a single solver keeps the default 32-byte layout; the
-    results are the same bit for bit."""
+    """Batch domains pack their rows (x = 1 on an 8-byte boundary, rows sized
+    for 8-byte vectors, 8-byte row pitch) while a single solver keeps the
+    default 32-byte layout; the results are the same bit for bit."""
     from cavityflow_cuda_gb300 import CLbmSolverGB300, LbmBatch
     from cavityflow_cuda_gb300.workloads import lattice_tau
 
@@ -88,8 +88,8 @@ def test_batch_packed_rows(gpu, storage):
     with LbmBatch(doms, storage=storage) as b:
         b.run(33)
         views = [b.domain(i) for i in range(len(doms))]
-        assert all(v.info()["x1_column"] * elem == 16 for v in views)
-        assert all(v.info()["row_pitch"] * elem % 16 == 0 for v in views)
+        assert all(v.info()["x1_column"] * elem == 8 for v in views)
+        assert all(v.info()["row_pitch"] * elem % 8 == 0 for v in views)
         got = [v.get_all() for v in views]
     for i, (size, inv_tau, lid) in enumerate(doms):
         with CLbmSolverGB300(size, inv_tau, lid, storage=storage) as s:
