@@ -713,8 +713,8 @@ def run_gpu(a):
         algo = bytes_per_lup * float(n) ** 3
         achieved = algo / (avg[dom] / 1e3) / 1e9
         info = s.info()
-        kname = f"{dom}_fast" + ({1: "_blk", 2: "_direct"}.get(info["beta_block_exchange"], "") if dom == "beta"
-                                 else "")
+        kname = f"{dom}_fast" + ({1: "_blk", 2: "_direct", 3: "_pk"}.get(info["beta_block_exchange"], "")
+                                 if dom == "beta" else "")
         if info["fast_variant"] >= s._lib.lbm_register_variant_count():  # the bulk-copy variants follow
             kname = "step_tma"
         traffic = profile_traffic(a, kname)
