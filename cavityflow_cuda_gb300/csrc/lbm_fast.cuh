@@ -636,144 +636,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_pk(typename St::bits* _
                                  step_of<St>(step_base, step_off));
 }
 
-// The packed beta with its loads as above (each shifted window as the aligned
-// vector plus one element) and its stores as whole aligned vectors: of a
-// shifted slot's aligned vector, the element that belongs to the
-// neighbouring group (a window's first element for c_x = +1, its last for
-// c_x = -1) is that lane's result, which a warp shuffle brings over as the
-// float its store would convert (dither already added), so each pair is
-// still one paired conversion.  Lanes at a warp or row edge store the
-// element the shuffle cannot reach with a 2-byte store, the way
-// beta_cells does.  Four cells per thread; all 32 lanes of the warp call it
-// together with consecutive groups, lanes past the domain's end too (they
-// read a valid group and never store).
-template <class St>
-__device__ __forceinline__ void beta_cells_pkx(typename St::bits* __restrict__ dd, const Grid& g,
-                                               const typename St::T inv_tau, const typename St::T lid_u,
-                                               const int lid_y, const int wall_y, const Cells c,
-                                               const uint32_t step)
-{
-    static_assert(sizeof(typename St::bits) == 2, "16-bit storage only");
-    constexpr int CPT = 4;
-    const int G = (g.nx + CPT - 1) / CPT;
-    const bool active = c.active;
-    const int lane = threadIdx.x & 31;
-    const int gi = c.gi, y = c.y, z = c.z;
-    const int x0 = 1 + gi * CPT;
-    const int nvalid = g.nx - x0 + 1;
-    const long long base = g.idx(x0, y, z);
-    // the neighbouring group of the same row is held by the adjacent lane
-    const bool left_in = gi > 0 && lane > 0;
-    const bool right_in = gi < G - 1 && lane < 31;
-    uint32_t w[Q][kPkMaxWords];
-    static_for<0, Q>([&](auto kc) {
-        constexpr int k = decltype(kc)::value;
-        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
-        pk_load<CPT, dir_x(k), true>(dd + rb, w[k]);
-    });
-    const bool lid = (y == lid_y);
-    const bool wall = (y == wall_y);
-    const float du = wall_shift<St>(lid_u);
-    const uint32_t row_hash = St::stochastic ? sr_hash((uint32_t)g.ref(0, y, z), step) : 0u;
-    float pend[Q];  // c_x = 0: the first cell of a pair; shifted slots: cell 0's result
-    float last[Q];  // shifted slots: cell 3's result
-    static_for<0, CPT>([&](auto vc) {
-        constexpr int v = decltype(vc)::value;
-        const bool valid = v < nvalid;
-        float cc[Q];
-        static_for<0, Q>([&](auto kc) {
-            constexpr int k = decltype(kc)::value;
-            using P = PkSlot<CPT, dir_x(k)>;
-            cc[opp(k)] = pk_in<St>(w[k][P::in_word(v, true)], P::in_half(v, true));
-        });
-        if (valid) {
-            if (wall) wall_correct(cc, du);
-            if (lid) inject_step<St>(cc, 0.0f, lid_u);
-            else collide<St>(cc, inv_tau);
-        } else {  // a cell past the row's end: every slot gets back the value read from it
-#pragma unroll
-            for (int k = 0; k < Q - 1; k += 2) {
-                const float t = cc[k];
-                cc[k] = cc[k + 1];
-                cc[k + 1] = t;
-            }
-        }
-        uint32_t h = 0;
-        if constexpr (St::stochastic) h = sr_cell(row_hash, x0 + v);
-        static_for<0, Q>([&](auto kc) {
-            constexpr int k = decltype(kc)::value;
-            constexpr int cx = dir_x(k);
-            const float d = valid ? pk_pre<St>(cc[k], h, k) : cc[k];
-            if constexpr (cx == 0) {  // aligned vector = cells (0,1), (2,3)
-                if constexpr ((v & 1) == 0) pend[k] = d;
-                else w[k][v >> 1] = pk_two<St>(pend[k], d);
-            } else if constexpr (v == 0) {
-                pend[k] = d;
-            } else if constexpr (v == 1) {
-                last[k] = d;  // waits for cell 2
-            } else if constexpr (v == 2) {
-                // c_x = +1: aligned (prev c3, c0 | c1, c2); c_x = -1: aligned (c1, c2 | c3, next c0)
-                w[k][cx > 0 ? 1 : 0] = pk_two<St>(last[k], d);
-            } else {
-                last[k] = d;
-            }
-        });
-    });
-    static_for<0, Q>([&](auto kc) {
-        constexpr int k = decltype(kc)::value;
-        constexpr int cx = dir_x(k);
-        const long long rb = base + (k * g.S + dir_z(k) * g.PY + dir_y(k) * g.P);  // slot offset: uniform
-        auto* const p = dd + rb;
-        if constexpr (cx == 0) {
-            if (active) *reinterpret_cast<uint2*>(p) = make_uint2(w[k][0], w[k][1]);
-        } else if constexpr (cx == 1) {
-            // loaded: w0 = (e0, e1), w1 = (e2, e3), w2 = e4; stored: e0..e3 = (prev c3, c0, c1, c2), e4 = c3
-            const float from_left = __shfl_up_sync(0xffffffffu, last[k], 1);
-            if (active) {
-                if (left_in) {
-                    *reinterpret_cast<uint2*>(p) = make_uint2(pk_two<St>(from_left, pend[k]), w[k][1]);
-                } else if (gi == 0) {  // e0 is the halo cell's, written back unchanged
-                    *reinterpret_cast<uint2*>(p) = make_uint2((w[k][0] & 0xffffu) | (pk_one<St>(pend[k]) << 16), w[k][1]);
-                } else {  // e0 is stored by the previous warp's last lane
-                    p[1] = (unsigned short)pk_one<St>(pend[k]);
-                    *reinterpret_cast<uint32_t*>(p + 2) = w[k][1];
-                }
-                if (!right_in && nvalid >= CPT) p[CPT] = (unsigned short)pk_one<St>(last[k]);
-            }
-        } else {
-            // loaded: w0 = e(-1), w1 = (e0, e1), w2 = (e2, e3); stored: e(-1) = c0, e0..e3 = (c1, c2, c3, next c0)
-            const float from_right = __shfl_down_sync(0xffffffffu, pend[k], 1);
-            if (active) {
-                if (right_in) {
-                    *reinterpret_cast<uint2*>(p) = make_uint2(w[k][0], pk_two<St>(last[k], from_right));
-                } else if (gi == G - 1) {  // e3 pulls for a cell past the row: written back unchanged
-                    *reinterpret_cast<uint2*>(p) =
-                        make_uint2(w[k][0], pk_one<St>(last[k]) | (w[k][2] & 0xffff0000u));
-                } else {  // e3 is stored by the next warp's first lane
-                    *reinterpret_cast<uint32_t*>(p) = w[k][0];
-                    p[2] = (unsigned short)pk_one<St>(last[k]);
-                }
-                if (!left_in) p[-1] = (unsigned short)pk_one<St>(pend[k]);
-            }
-        }
-    });
-}
-
-template <class St, int BLOCK, int MINB>
-__global__ void __launch_bounds__(BLOCK, MINB) beta_fast_pkx(typename St::bits* __restrict__ dd, const Grid g,
-                                                             const typename St::T inv_tau,
-                                                             const typename St::T lid_u, const int lid_y,
-                                                             const int wall_y,
-                                                             const uint32_t* __restrict__ step_base,
-                                                             const uint32_t step_off, const FastDiv divG,
-                                                             const int z_base)
-{
-    const int G = (g.nx + 3) / 4;
-    beta_cells_pkx<St>(dd, g, inv_tau, lid_u, lid_y, wall_y,
-                       cells_of_plane(g, G, divG, blockIdx.x * BLOCK + threadIdx.x, z_base + (int)blockIdx.y + 1),
-                       step_of<St>(step_base, step_off));
-}
-
 template <class St, int CPT, int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB) beta_fast_direct(typename St::bits* __restrict__ dd, const Grid g,
                                                                 const typename St::T inv_tau,
@@ -1018,9 +880,7 @@ cudaError_t launch_fast_variant(bool alpha, void* dd, const Grid& g, const Param
     }
     constexpr KernelShape k = fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    if constexpr (fv.packed == 3 && sizeof(typename St::bits) == 2 && CPT == 4)
-        return launch(beta_fast_pkx<St, k.block, k.minb>, CPT, k.block);
-    else if constexpr (fv.packed != 0 && fv.packed != 3 && sizeof(typename St::bits) == 2)
+    if constexpr (fv.packed != 0 && sizeof(typename St::bits) == 2)
         return launch(beta_fast_pk<St, CPT, k.block, k.minb, fv.packed == 2>, CPT, k.block);
     else if constexpr (fv.direct) return launch(beta_fast_direct<St, CPT, k.block, k.minb>, CPT, k.block);
     else if constexpr (fv.block_exchange) return launch(beta_fast_blk<St, CPT, k.block, k.minb>, CPT, k.block);
@@ -1122,8 +982,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // the block-wide barriers of the exchanging beta body are reached uniformly.
 // kBeta: 0 warp exchange (beta_cells), 1 block exchange (beta_cells_blk),
 // 2 direct windows (beta_cells_direct), 3 and 4 packed 16-bit windows
-// (beta_cells_pk with piece or vector loads), 5 packed 16-bit windows with
-// exchanged stores (beta_cells_pkx).
+// (beta_cells_pk with piece or vector loads).
 template <class St, int CPT, int BLOCK, int MINB, bool kAlpha, int kBeta>
 __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __restrict__ pool,
                                                           const BatchDomain* __restrict__ doms,
@@ -1162,7 +1021,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) batch_step(typename St::bits* __r
         const T inv_tau = T(d.inv_tau), lid_u = T(d.lid_u);
         const int lid_y = d.lid_y, wall_y = d.wall_y;
         if constexpr (kAlpha) alpha_cells<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
-        else if constexpr (kBeta == 5) beta_cells_pkx<St>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
         else if constexpr (kBeta >= 3) beta_cells_pk<St, CPT, kBeta == 4>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
         else if constexpr (kBeta == 2) beta_cells_direct<St, CPT>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
         else if constexpr (kBeta == 1) beta_cells_blk<St, CPT, BLOCK>(dd, g, inv_tau, lid_u, lid_y, wall_y, c, ds);
@@ -1176,7 +1034,7 @@ cudaError_t launch_batch_kernel(const BatchArgs& a, cudaStream_t st)
     constexpr FastVariant fv = kFastMenu[VARIANT];
     constexpr KernelShape k = kAlpha ? fv.alpha : fv.beta;
     constexpr int CPT = shape_cpt<St>(k);
-    constexpr bool pk = fv.packed != 0 && sizeof(typename St::bits) == 2 && (fv.packed != 3 || CPT == 4);
+    constexpr bool pk = fv.packed != 0 && sizeof(typename St::bits) == 2;
     auto kern = batch_step<St, CPT, k.block, k.minb, kAlpha,
                            pk ? 2 + fv.packed : fv.direct ? 2 : fv.block_exchange ? 1 : 0>;
     int dev = 0, sms = 0, per_sm = 0;

@@ -63,9 +63,7 @@ struct KernelShape {
 // `packed` (16-bit storage; other storages run the direct beta): the direct
 // windows with two cells per 32-bit word and paired conversions
 // (beta_fast_pk), loading each window as its pieces (1) or as the aligned
-// vector plus one element (2); 3: those loads, and stores of whole aligned
-// vectors whose element from the neighbouring group comes by warp shuffle
-// (beta_fast_pkx, 8-byte beta vectors).
+// vector plus one element (2).
 struct FastVariant {
     KernelShape alpha;
     KernelShape beta;
@@ -73,7 +71,7 @@ struct FastVariant {
     bool direct = false;
     int packed = 0;
 };
-constexpr int kRegisterVariants = 26;
+constexpr int kRegisterVariants = 24;
 constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 256, 1}, {1, 256, 1}, false},  // 16-byte vectors, registers unconstrained
     {{1, 256, 2}, {1, 256, 2}, false},  // 16-byte vectors, <= 128 registers
@@ -99,8 +97,6 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 64, 4}, {2, 64, 8}, false, true, 2},   // the same, <= 128 registers
     {{2, 64, 8}, {2, 64, 10}, false, true, 1},  // 8-byte alpha and packed beta (fit the packed batch rows)
     {{2, 64, 8}, {2, 64, 10}, false, true, 2},  // the same, vector loads
-    {{1, 64, 4}, {2, 64, 8}, false, true, 3},   // alpha 16-byte; beta packed, vector loads and stores
-    {{1, 64, 4}, {2, 64, 10}, false, true, 3},  // the same, <= 102 registers
 };
 struct TmaConfig {
     int rows;            // rows per work unit

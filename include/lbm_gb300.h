@@ -309,11 +309,11 @@ int lbm_selftest_bounded_wait(lbm_solver* solver, int32_t limit_us);
 /* ---- tuning (no counterpart in the reference, whose block shape comes from
  * the XML gpu/grid-configuration, src/CConfiguration.cpp:150-160) ---------- */
 
-/* Number of launch variants of the box-cavity kernels: 26 register-blocked
- * vector kernels (0..25: cells per thread, threads per block and blocks per
+/* Number of launch variants of the box-cavity kernels: 24 register-blocked
+ * vector kernels (0..23: cells per thread, threads per block and blocks per
  * SM of the alpha and the beta kernel, and whether beta exchanges edge
- * elements per warp, per block or not at all; 18..25 keep 16-bit populations
- * two cells per register) and 6 row-pipelined bulk-copy kernels (26..31: rows
+ * elements per warp, per block or not at all; 18..23 keep 16-bit populations
+ * two cells per register) and 6 row-pipelined bulk-copy kernels (24..29: rows
  * per unit, buffers, consumer warps). */
 int lbm_fast_variant_count(void);
 /* Number of register variants (the first variants; the batch kernel's menu). */

@@ -128,10 +128,10 @@ def test_cli_usage_and_argument_errors(lib, tmp_path):
 
 
 def test_launch_variant_menu_size(lib):
-    """26 register variants (0-25) and 6 bulk-copy variants (26-31); the GPU
+    """24 register variants (0-23) and 6 bulk-copy variants (24-29); the GPU
     parity tests enumerate exactly these."""
-    assert lib.lbm_fast_variant_count() == 32
-    assert lib.lbm_register_variant_count() == 26
+    assert lib.lbm_fast_variant_count() == 30
+    assert lib.lbm_register_variant_count() == 24
 
 
 def test_batch_and_server_arguments_checked_before_the_device(lib):

@@ -39,7 +39,7 @@ def oracle_run(oracle, n, storage, itau, lid, steps):
 
 
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16s", "bf16s", "f16sr"])
-@pytest.mark.parametrize("variant", range(32))
+@pytest.mark.parametrize("variant", range(30))
 def test_moving_wall_matches_oracle_every_variant(gpu, oracle, storage, variant):
     from cavityflow_cuda_gb300 import LbmError
 
