@@ -51,7 +51,7 @@ int default_variant(int storage);
 int default_batch_variant(int storage);
 // Creates a solver; with `external_dd` its populations live there (a batch
 // pool) and are initialised but never freed by the solver.
-// x1_align: 32 (the default layout) or 16 (the packed rows of batch pools,
+// x1_align: 32 (the default layout) or 8 (the packed rows of batch pools,
 // see make_grid).
 int create_solver(const lbm_params* prm, void* external_dd, lbm_solver** out, int x1_align = 32);
 void destroy_solver(lbm_solver* s);
