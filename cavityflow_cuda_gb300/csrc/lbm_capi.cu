@@ -90,12 +90,16 @@ constexpr int kGraphPairs = 32;  // alpha/beta pairs per captured graph
 // Batch and server rows are packed for 8-byte vectors (kPackedX1Align), so
 // their variants use 8-byte (or narrower) vectors in both kernels.  On the
 // seeded 512-cavity workload the direct beta windows in two-warp blocks
-// (variant 13) are fastest for FP32 and the FP16 storages, the FP64 warp
-// exchange (3) for FP64.
+// (variant 13) are fastest for FP32, the packed 16-bit beta at <= 128
+// registers (22: the batch kernel's own state spills the 102-register
+// shape) for the 16-bit storages, the FP64 warp exchange (3) for FP64.
 int lbm_detail::default_batch_variant(int storage)
 {
     switch (storage) {
     case LBM_STORAGE_F64: return 3;
+    case LBM_STORAGE_F16S:
+    case LBM_STORAGE_BF16S:
+    case LBM_STORAGE_F16SR: return 22;
     default: return 13;
     }
 }

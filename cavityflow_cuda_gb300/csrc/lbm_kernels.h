@@ -95,8 +95,8 @@ constexpr FastVariant kFastMenu[kRegisterVariants] = {
     {{1, 64, 4}, {2, 64, 8}, false, true, 1},   // the same, <= 128 registers
     {{1, 64, 4}, {2, 64, 10}, false, true, 2},  // alpha 16-byte; beta 8-byte packed, vector loads
     {{1, 64, 4}, {2, 64, 8}, false, true, 2},   // the same, <= 128 registers
-    {{2, 64, 8}, {2, 64, 10}, false, true, 1},  // 8-byte alpha and packed beta (fit the packed batch rows)
-    {{2, 64, 8}, {2, 64, 10}, false, true, 2},  // the same, vector loads
+    {{2, 64, 8}, {2, 64, 8}, false, true, 2},   // 8-byte alpha, packed beta with vector loads, <= 128 registers
+    {{2, 64, 8}, {2, 64, 10}, false, true, 2},  // the same, <= 102 registers (22 and 23 fit the batch rows)
 };
 struct TmaConfig {
     int rows;            // rows per work unit
