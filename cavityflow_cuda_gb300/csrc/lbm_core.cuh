@@ -169,7 +169,17 @@ struct BF16S {
     using T = float;
     static constexpr bool shifted = true;
     static constexpr bool stochastic = false;
-    __device__ static T load(bits b) { return __bfloat162float(__ushort_as_bfloat16(b)); }
+    // Widening as the mixed-precision add b + (-0.0f), which is exact (zeros
+    // keep their sign, subnormals stay): it reads a bfloat16 half of a
+    // register in place, as the FP16 conversions do, where a shift into a
+    // register of its own per element took the 8-cell alpha from 168 to 239
+    // registers.
+    __device__ static T load(bits b)
+    {
+        float r;
+        asm("add.rn.f32.bf16 %0, %1, %2;" : "=f"(r) : "h"(b), "f"(-0.0f));
+        return r;
+    }
     __device__ static bits store(T v) { return __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
     __device__ static T load_step(bits b) { return load(b); }
     static constexpr int kStepLog2 = 0;
