@@ -146,10 +146,14 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     *out = nullptr;
     if (storage < LBM_STORAGE_F64 || storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", storage);
+    long long pool_cells = 0;  // halo included; bounded like one domain, so the pool's byte count cannot overflow
     for (int i = 0; i < count; ++i) {
-        for (int d = 0; d < 3; ++d)
-            if (domains[i].size[d] <= 0 || domains[i].size[d] > (1 << 20))
-                return fail(LBM_ERR_INVALID_ARGUMENT, "domain %d: size must be in [1, 2^20]", i);
+        if (!domain_size_ok(domains[i].size))
+            return fail(LBM_ERR_INVALID_ARGUMENT, "domain %d: size must be in [1, 2^20] per axis and at most 2^40 cells",
+                        i);
+        pool_cells += ((long long)domains[i].size[0] + 2) * (domains[i].size[1] + 2) * (domains[i].size[2] + 2);
+        if (pool_cells > kMaxDomainCells)
+            return fail(LBM_ERR_INVALID_ARGUMENT, "the batch's domains hold more than 2^40 cells");
         if (!(domains[i].inv_tau > 0) || !std::isfinite(domains[i].inv_tau) || !std::isfinite(domains[i].lid_velocity))
             return fail(LBM_ERR_INVALID_ARGUMENT, "domain %d: inv_tau must be positive and finite", i);
     }

@@ -429,9 +429,8 @@ int lbm_detail::create_solver(const lbm_params* prm, void* external_dd, lbm_solv
 {
     if (!prm || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
-    for (int d = 0; d < 3; ++d)
-        if (prm->size[d] <= 0 || prm->size[d] > (1 << 20))
-            return fail(LBM_ERR_INVALID_ARGUMENT, "domain size must be in [1, 2^20]");
+    if (!domain_size_ok(prm->size))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "domain size must be in [1, 2^20] per axis and at most 2^40 cells");
     if (prm->storage < LBM_STORAGE_F64 || prm->storage > LBM_STORAGE_F16SR)
         return fail(LBM_ERR_INVALID_ARGUMENT, "unknown storage %d", prm->storage);
     for (int f = 0; f < 6; ++f)

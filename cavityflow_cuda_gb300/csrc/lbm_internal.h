@@ -61,4 +61,20 @@ int* err_flag(lbm_solver* s);
 uint32_t* step_words(lbm_solver* s);
 int check_kernel_flag(lbm_solver* s);
 
+// Largest domain any entry point accepts, halo included: 2^40 cells, far
+// beyond device memory (8 bytes x 19 slots x 2^40 cells is 167 TB) and small
+// enough that no element or byte count derived from it overflows 64 bits.
+constexpr long long kMaxDomainCells = 1LL << 40;
+// Each axis in [1, 2^20] and (nx+2)(ny+2)(nz+2) <= kMaxDomainCells.
+inline bool domain_size_ok(const int32_t size[3])
+{
+    long long cells = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (size[d] <= 0 || size[d] > (1 << 20)) return false;
+        cells *= (long long)size[d] + 2;  // < 2^40 * (2^20 + 3) < 2^63
+        if (cells > kMaxDomainCells) return false;
+    }
+    return true;
+}
+
 }  // namespace lbm_detail

@@ -422,9 +422,8 @@ int lbm_server_destroy(lbm_server* s)
 int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
 {
     if (!s || !req) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
-    for (int d = 0; d < 3; ++d)
-        if (req->size[d] <= 0 || req->size[d] > (1 << 20))
-            return fail(LBM_ERR_INVALID_ARGUMENT, "size must be in [1, 2^20]");
+    if (!domain_size_ok(req->size))
+        return fail(LBM_ERR_INVALID_ARGUMENT, "size must be in [1, 2^20] per axis and at most 2^40 cells");
     if (req->steps < 0) return fail(LBM_ERR_INVALID_ARGUMENT, "negative step count");
     if (!(req->inv_tau > 0) || !std::isfinite(req->inv_tau) || !std::isfinite(req->lid_velocity))
         return fail(LBM_ERR_INVALID_ARGUMENT, "inv_tau must be positive and finite");

@@ -176,7 +176,10 @@ int lbm_configuration_physical(const lbm_configuration* config, lbm_physical* ou
 
 /* Creation parameters of one solver. */
 typedef struct lbm_params {
-    int32_t size[3];            /* interior cells nx, ny, nz (domain-size)     */
+    int32_t size[3];            /* interior cells nx, ny, nz (domain-size):
+                                   each in [1, 2^20], (nx+2)(ny+2)(nz+2) at
+                                   most 2^40 (batches: all domains together,
+                                   servers: each request)                      */
     int32_t storage;            /* lbm_storage                                 */
     int32_t boundary[6];        /* face flags: -x, +x, -y, +y, -z, +z
                                    (src/CLbmSolver.hpp:36-45)                  */

@@ -144,8 +144,10 @@ def test_batch_and_server_arguments_checked_before_the_device(lib):
     from cavityflow_cuda_gb300 import LbmBatch, LbmError, LbmServer
 
     good = [((8, 8, 8), 1.6, 0.05), ((5, 6, 7), 1.2, 0.02)]
+    big = ((1 << 19, 1 << 19, 1), 1.6, 0.05)  # 0.8 * 2^40 cells with its halo: accepted alone
     for bad in ([((8, 0, 8), 1.6, 0.05)], [((8, 8, 8), 0.0, 0.05)], [((8, 8, 8), math.inf, 0.05)],
-                [((8, 8, 8), 1.6, math.nan)], [((8, 8, (1 << 20) + 1), 1.6, 0.05)]):
+                [((8, 8, 8), 1.6, math.nan)], [((8, 8, (1 << 20) + 1), 1.6, 0.05)],
+                [((1 << 20, 1 << 20, 1 << 20), 1.6, 0.05)], [big, big]):  # a domain, or the pool, above 2^40 cells
         with pytest.raises(LbmError) as ei:
             LbmBatch(good + bad, storage="f32")
         assert ei.value.status == 1, bad
@@ -154,9 +156,10 @@ def test_batch_and_server_arguments_checked_before_the_device(lib):
             LbmServer(storage="f32", **kw)
         assert ei.value.status == 1, kw
     if not torch.cuda.is_available():
-        with pytest.raises(LbmError) as ei:
-            LbmBatch(good, storage="f16sr")
-        assert ei.value.status == 10
+        for ok in (good, good + [big]):
+            with pytest.raises(LbmError) as ei:
+                LbmBatch(ok, storage="f16sr")
+            assert ei.value.status == 10
         with pytest.raises(LbmError) as ei:
             LbmServer(budget_bytes=1 << 30, storage="f16s")
         assert ei.value.status == 10
@@ -165,6 +168,8 @@ def test_batch_and_server_arguments_checked_before_the_device(lib):
 @pytest.mark.parametrize("kw,status", [
     (dict(size=(0, 8, 8)), 1),
     (dict(size=(8, 8, (1 << 20) + 1)), 1),
+    (dict(size=(1 << 20, 1 << 20, 1 << 20)), 1),  # more than 2^40 cells: byte counts would overflow
+    (dict(size=(1 << 19, 1 << 19, 2)), 1),        # (2^19 + 2)^2 * 4 > 2^40 cells
     (dict(boundary=(1, 1, 1, 1, 16, 1)), 1),
     (dict(inv_tau=0.0), 1),
     (dict(inv_tau=float("nan")), 1),
