@@ -945,7 +945,7 @@ const char* lbm_status_string(int status)
     case LBM_ERR_CUDA: return "CUDA error";
     case LBM_ERR_OUT_OF_MEMORY: return "out of memory";
     case LBM_ERR_UNSUPPORTED: return "unsupported";
-    case LBM_ERR_CONFIG: return "no stable time step for the configuration";
+    case LBM_ERR_CONFIG: return "configuration error (rejected file or no stable time step)";
     case LBM_ERR_IO: return "I/O error";
     case LBM_ERR_BUDGET: return "over memory budget";
     case LBM_ERR_NOT_READY: return "not ready";

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <fstream>
 #include <limits>
 #include <memory>
@@ -46,7 +47,7 @@ public:
     bool parse(Node& root, std::string& err)
     {
         skip_misc();
-        if (!element(root, err)) return false;
+        if (!element(root, err, 0)) return false;
         skip_misc();
         if (i_ != s_.size()) {
             err = "trailing content after the root element";
@@ -86,8 +87,16 @@ private:
         }
     }
 
-    bool element(Node& n, std::string& err)
+    // The schema nests four levels deep; deeper documents are refused rather
+    // than recursed into without bound.
+    static constexpr int kMaxDepth = 64;
+
+    bool element(Node& n, std::string& err, int depth)
     {
+        if (depth > kMaxDepth) {
+            err = "elements nested deeper than 64 levels";
+            return false;
+        }
         if (i_ >= s_.size() || s_[i_] != '<') {
             err = "expected an element";
             return false;
@@ -132,6 +141,10 @@ private:
                 i_ += 2;
                 const size_t b2 = i_;
                 while (i_ < s_.size() && s_[i_] != '>') ++i_;
+                if (i_ >= s_.size()) {
+                    err = "unterminated </" + n.name + ">";
+                    return false;
+                }
                 std::string close = s_.substr(b2, i_ - b2);
                 while (!close.empty() && std::isspace((unsigned char)close.back())) close.pop_back();
                 if (close != n.name) {
@@ -143,7 +156,7 @@ private:
             }
             if (s_[i_] == '<') {
                 auto c = std::make_unique<Node>();
-                if (!element(*c, err)) return false;
+                if (!element(*c, err, depth + 1)) return false;
                 n.children.push_back(std::move(c));
             } else {
                 const size_t e = s_.find('<', i_);
@@ -200,9 +213,10 @@ void str(const Node* root, std::initializer_list<const char*> path, std::string&
 
 }  // namespace
 
-extern "C" int lbm_read_configuration(const char* path, lbm_configuration* c)
+namespace {
+
+int read_configuration(const char* path, lbm_configuration* c)
 {
-    if (!path || !c) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(LBM_ERR_IO, "cannot open configuration \"%s\"", path);
     std::stringstream ss;
@@ -282,6 +296,18 @@ extern "C" int lbm_read_configuration(const char* path, lbm_configuration* c)
     }
     if (bad) return fail(LBM_ERR_CONFIG, "%s: %s", path, bad);
     return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" int lbm_read_configuration(const char* path, lbm_configuration* c)
+{
+    if (!path || !c) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
+    try {  // no C++ exception may cross the C interface (a file too large for memory, say)
+        return read_configuration(path, c);
+    } catch (const std::exception& e) {
+        return fail(LBM_ERR_CONFIG, "%s: %s", path, e.what());
+    }
 }
 
 extern "C" int lbm_configuration_physical(const lbm_configuration* c, lbm_physical* out)

@@ -48,7 +48,8 @@ typedef enum lbm_status {
     LBM_ERR_CUDA = 3,             /* a CUDA runtime call or launch failed          */
     LBM_ERR_OUT_OF_MEMORY = 4,    /* device or pinned-host allocation failed       */
     LBM_ERR_UNSUPPORTED = 5,      /* valid request this build does not provide     */
-    LBM_ERR_CONFIG = 6,           /* no stable time step (reference: exit())       */
+    LBM_ERR_CONFIG = 6,           /* no stable time step (reference: exit()), or a
+                                     configuration file the reader rejects        */
     LBM_ERR_IO = 7,               /* file could not be read or written             */
     LBM_ERR_BUDGET = 8,           /* request does not fit the memory budget        */
     LBM_ERR_NOT_READY = 9,        /* result requested before it exists             */

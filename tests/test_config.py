@@ -104,6 +104,26 @@ def test_reader_reports_missing_elements_and_files(lib, tmp_path):
     assert ei.value.status in (6, 7)
 
 
+@pytest.mark.parametrize("text", [
+    "<lbm-configuration></lbm-configuration",          # closing tag cut off at the end of the file
+    "<lbm-configuration><grid></grid",
+    "<lbm-configuration><grid/><x",                    # unterminated start tag
+    "<a>" * 100 + "</a>" * 100,                       # nested deeper than the reader follows
+    "",
+    "<",
+])
+def test_reader_rejects_malformed_xml(lib, tmp_path, text):
+    """Malformed documents are configuration errors (LBM_ERR_CONFIG), never a
+    read past the end of the text or an unbounded recursion."""
+    from cavityflow_cuda_gb300 import LbmError, read_configuration
+
+    p = tmp_path / "malformed.xml"
+    p.write_text(text)
+    with pytest.raises(LbmError) as ei:
+        read_configuration(str(p))
+    assert ei.value.status == 6, text[:40]
+
+
 def test_reader_ignores_subdomain_num_as_the_serial_reference(lib, tmp_path):
     from cavityflow_cuda_gb300 import read_configuration
 
