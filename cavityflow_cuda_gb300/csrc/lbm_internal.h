@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cstdint>
+#include <exception>
+#include <new>
 #include <cuda_runtime.h>
 
 #include "../../include/lbm_gb300.h"
@@ -60,6 +62,21 @@ int* err_flag(lbm_solver* s);
 // [1] always zero (the base of directly launched steps).
 uint32_t* step_words(lbm_solver* s);
 int check_kernel_flag(lbm_solver* s);
+
+// Runs an entry point's body with C++ exceptions turned into status codes,
+// since none may cross the C interface: a host buffer too large for memory
+// (a checkpoint or VTK file of a big domain) throws std::bad_alloc.
+template <class Body>
+int guarded(const char* entry, Body&& body)
+{
+    try {
+        return body();
+    } catch (const std::bad_alloc&) {
+        return fail(LBM_ERR_OUT_OF_MEMORY, "%s: host allocation failed", entry);
+    } catch (const std::exception& e) {
+        return fail(LBM_ERR_IO, "%s: %s", entry, e.what());
+    }
+}
 
 // Largest domain any entry point accepts, halo included: 2^40 cells, far
 // beyond device memory (8 bytes x 19 slots x 2^40 cells is 167 TB) and small

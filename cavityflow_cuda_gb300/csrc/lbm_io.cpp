@@ -103,7 +103,7 @@ void be64(unsigned char* p, uint64_t v)
 
 extern "C" {
 
-int lbm_save_checkpoint(lbm_solver* s, const char* path)
+static int save_checkpoint_unguarded(lbm_solver* s, const char* path)
 {
     if (!s || !path) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     if (int r = lbm_synchronize(s)) return r;
@@ -169,7 +169,7 @@ static int read_header(FILE* f, const char* path, CkptHeader& h, CkptLid& lid)
     return LBM_OK;
 }
 
-int lbm_load_checkpoint(lbm_solver* s, const char* path)
+static int load_checkpoint_unguarded(lbm_solver* s, const char* path)
 {
     if (!s || !path) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     File in;
@@ -208,7 +208,7 @@ int lbm_load_checkpoint(lbm_solver* s, const char* path)
     return LBM_OK;
 }
 
-int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** out)
+static int create_from_checkpoint_unguarded(const char* path, int32_t device, lbm_solver** out)
 {
     if (!path || !out) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     *out = nullptr;
@@ -241,7 +241,7 @@ int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** ou
     return LBM_OK;
 }
 
-int lbm_write_vtk(lbm_solver* s, const char* path, const double length[3], int32_t binary)
+static int write_vtk_unguarded(lbm_solver* s, const char* path, const double length[3], int32_t binary)
 {
     if (!s || !path) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     const int nx = s->g.nx, ny = s->g.ny, nz = s->g.nz;
@@ -333,6 +333,26 @@ int lbm_write_vtk(lbm_solver* s, const char* path, const double length[3], int32
     }
     if (std::ferror(f)) return fail(LBM_ERR_IO, "error writing \"%s\"", path);
     return LBM_OK;
+}
+
+int lbm_save_checkpoint(lbm_solver* s, const char* path)
+{
+    return guarded("lbm_save_checkpoint", [&] { return save_checkpoint_unguarded(s, path); });
+}
+
+int lbm_load_checkpoint(lbm_solver* s, const char* path)
+{
+    return guarded("lbm_load_checkpoint", [&] { return load_checkpoint_unguarded(s, path); });
+}
+
+int lbm_create_from_checkpoint(const char* path, int32_t device, lbm_solver** out)
+{
+    return guarded("lbm_create_from_checkpoint", [&] { return create_from_checkpoint_unguarded(path, device, out); });
+}
+
+int lbm_write_vtk(lbm_solver* s, const char* path, const double length[3], int32_t binary)
+{
+    return guarded("lbm_write_vtk", [&] { return write_vtk_unguarded(s, path, length, binary); });
 }
 
 }  // extern "C"
