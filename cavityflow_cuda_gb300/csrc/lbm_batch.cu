@@ -140,7 +140,7 @@ void free_batch(lbm_batch* b)
 
 extern "C" {
 
-int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t storage, int32_t device, lbm_batch** out)
+static int batch_create_unguarded(const lbm_domain_spec* domains, int32_t count, int32_t storage, int32_t device, lbm_batch** out)
 {
     if (!domains || !out || count <= 0) return fail(LBM_ERR_INVALID_ARGUMENT, "domains, count and out are required");
     *out = nullptr;
@@ -223,6 +223,11 @@ int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t stor
     if (r) return bail(r);
     *out = b;
     return LBM_OK;
+}
+
+int lbm_batch_create(const lbm_domain_spec* domains, int32_t count, int32_t storage, int32_t device, lbm_batch** out)
+{
+    return guarded("lbm_batch_create", [&] { return batch_create_unguarded(domains, count, storage, device, out); });
 }
 
 int lbm_batch_destroy(lbm_batch* b)

@@ -588,7 +588,7 @@ int lbm_value_size(const lbm_solver* s)
     return s ? value_bytes(s->storage) : 0;
 }
 
-int lbm_set_driven_cavity(lbm_solver* s)
+static int set_driven_cavity_unguarded(lbm_solver* s)
 {
     if (int r = check_solver(s)) return r;
     if (s->lid_mode == LBM_LID_MOVING_WALL) {
@@ -601,6 +601,11 @@ int lbm_set_driven_cavity(lbm_solver* s)
     const int32_t size[3] = {s->g.nx, 1, s->g.nz};
     std::vector<int32_t> lid((size_t)s->g.nx * s->g.nz, LBM_VELOCITY_INJECTION);
     return lbm_set_flags(s, origin, size, lid.data());
+}
+
+int lbm_set_driven_cavity(lbm_solver* s)
+{
+    return guarded("lbm_set_driven_cavity", [&] { return set_driven_cavity_unguarded(s); });
 }
 
 int lbm_step_alpha(lbm_solver* s, void* stream)
@@ -849,7 +854,7 @@ int lbm_set_density_distributions(lbm_solver* s, const int32_t origin[3], const 
     return LBM_OK;
 }
 
-int lbm_get_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3], int32_t* host)
+static int get_flags_unguarded(lbm_solver* s, const int32_t origin[3], const int32_t size[3], int32_t* host)
 {
     if (int r = check_solver(s)) return r;
     if (!host) return fail(LBM_ERR_INVALID_ARGUMENT, "host buffer is NULL");
@@ -863,7 +868,12 @@ int lbm_get_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3],
     return LBM_OK;
 }
 
-int lbm_set_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3], const int32_t* host)
+int lbm_get_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3], int32_t* host)
+{
+    return guarded("lbm_get_flags", [&] { return get_flags_unguarded(s, origin, size, host); });
+}
+
+static int set_flags_unguarded(lbm_solver* s, const int32_t origin[3], const int32_t size[3], const int32_t* host)
 {
     if (int r = check_solver(s)) return r;
     if (!host) return fail(LBM_ERR_INVALID_ARGUMENT, "host buffer is NULL");
@@ -879,6 +889,11 @@ int lbm_set_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3],
     CK(copy_compact(s->flags, 1, s->g, o, n, tmp.data(), false), "cudaMemcpy3D flags");
     s->macros_fresh = false;
     return refresh_path(s);
+}
+
+int lbm_set_flags(lbm_solver* s, const int32_t origin[3], const int32_t size[3], const int32_t* host)
+{
+    return guarded("lbm_set_flags", [&] { return set_flags_unguarded(s, origin, size, host); });
 }
 
 static int macro_copy(lbm_solver* s, const int32_t* origin, const int32_t* size, void* host, int first, int count,

@@ -419,7 +419,7 @@ int lbm_server_destroy(lbm_server* s)
     return LBM_OK;
 }
 
-int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
+static int server_submit_unguarded(lbm_server* s, const lbm_request* req, int64_t* id)
 {
     if (!s || !req) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
     if (!domain_size_ok(req->size))
@@ -441,7 +441,12 @@ int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
     return LBM_OK;
 }
 
-int lbm_server_round(lbm_server* s, int32_t* ran)
+int lbm_server_submit(lbm_server* s, const lbm_request* req, int64_t* id)
+{
+    return guarded("lbm_server_submit", [&] { return server_submit_unguarded(s, req, id); });
+}
+
+static int server_round_unguarded(lbm_server* s, int32_t* ran)
 {
     if (!s) return fail(LBM_ERR_INVALID_ARGUMENT, "server is NULL");
     if (ran) *ran = 0;
@@ -553,6 +558,11 @@ int lbm_server_round(lbm_server* s, int32_t* ran)
     return LBM_OK;
 }
 
+int lbm_server_round(lbm_server* s, int32_t* ran)
+{
+    return guarded("lbm_server_round", [&] { return server_round_unguarded(s, ran); });
+}
+
 int lbm_server_poll(lbm_server* s, lbm_completion* out, int32_t capacity, int32_t* count)
 {
     if (!s || !count || (capacity > 0 && !out)) return fail(LBM_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -565,7 +575,7 @@ int lbm_server_poll(lbm_server* s, lbm_completion* out, int32_t capacity, int32_
     return LBM_OK;
 }
 
-int lbm_server_take_result(lbm_server* s, int64_t id, void* rho_host, void* u_host)
+static int server_take_result_unguarded(lbm_server* s, int64_t id, void* rho_host, void* u_host)
 {
     if (!s) return fail(LBM_ERR_INVALID_ARGUMENT, "server is NULL");
     auto it = s->finished.find(id);
@@ -577,6 +587,11 @@ int lbm_server_take_result(lbm_server* s, int64_t id, void* rho_host, void* u_ho
     s->finished.erase(it);
     delete r;
     return status;
+}
+
+int lbm_server_take_result(lbm_server* s, int64_t id, void* rho_host, void* u_host)
+{
+    return guarded("lbm_server_take_result", [&] { return server_take_result_unguarded(s, id, rho_host, u_host); });
 }
 
 int lbm_server_get_stats(const lbm_server* s, lbm_server_stats* st)
