@@ -9,6 +9,7 @@
 // graph of captured alpha/beta pairs.
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <vector>
 
@@ -164,6 +165,13 @@ static int batch_create_unguarded(const lbm_domain_spec* domains, int32_t count,
 
     lbm_batch* b = new (std::nothrow) lbm_batch();
     if (!b) return fail(LBM_ERR_OUT_OF_MEMORY, "host allocation failed");
+    struct FreeIfThrown {  // a host allocation that throws below (turned into a status by
+        lbm_batch* b;      // lbm_batch_create) must not leak the batch's device memory
+        ~FreeIfThrown()
+        {
+            if (std::uncaught_exceptions() > 0) free_batch(b);
+        }
+    } free_if_thrown{b};
     b->storage = storage;
     b->device = device;
     b->variant = default_batch_variant(storage);
